@@ -1,0 +1,267 @@
+"""Benchmark: Mpath-samples/s of the GPU MIS volumetric path tracer on the 1080p many-light terrain.
+
+Workload (one step = one frame): 1920x1080, 64 spp, max depth 6, 2,093,058-triangle heightfield with
+10,000 emissive triangles sampled through the light tree and a sky environment light; seeded
+synthetic scene (no external assets exist).  Scene data (~250 MB) is larger than the 129 MB L2 and L2
+is additionally flushed between timed steps.
+
+  value   device-resident throughput: K frames launched back to back on one stream, CUDA events
+  e2e     the same metric through lgpu_render with a host film (H2D + D2H film copies inside)
+  roofline  algorithmic BVH bytes (node + triangle records fetched, counted in-kernel by a separate
+          counting launch of the same frame) / kernel time, against the measured HBM copy peak
+  cpu_baseline  the CPU oracle (restatement of the reference integrator) on this host's cores over
+          a bounded stratified sample of the same frame
+
+--impl reference runs that CPU path alone with all host threads on the same config and metric.
+Multi-GPU (torchrun, N > 1): replicas -- every rank renders its own frame (seed = rank); no
+collective on the data path; value = all ranks' paths / max time.
+"""
+import argparse
+import json
+import os
+import pathlib
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpath-samples/s at 1080p, equal relMSE: batched vs plain GPU vs CPU; bwd/fwd ratio"
+UNIT = "Mpath-samples/s"
+WORKLOAD = dict(workload="many-light terrain (2.1M tris, 10k emitters, sky env), MIS volumetric path tracing",
+                width=1920, height=1080, spp=64, max_depth=6, triangles=2093058 + 10000, emitters=10000,
+                spectral="RGB3", light_sampler="light tree")
+# DRAM bytes per launch of the render kernel from one ncu capture (profiles/render_terrain_1080p.md),
+# scaled to the full frame; None until captured.
+NCU_TRAFFIC_PER_LAUNCH = None
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--spp", type=int, default=64)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        res = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        sm = []
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                res["sm_max_mhz"] = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except Exception:
+                pass
+        if sm:
+            res["sm_mhz"] = float(np.median(sm))
+        res["reasons"] = sorted(reasons)
+        res["samples"] = len(sm)
+        return res
+
+
+def cpu_baseline(sb, cam, opts, seconds, threads=0):
+    """Oracle throughput on a stratified pixel sample at full spp (bounded to ~`seconds`)."""
+    from oracle.oracle import Oracle
+    o = Oracle(sb)
+    W, H, spp = opts.width, opts.height, opts.spp
+    threads = threads or os.cpu_count()
+
+    def ids_for(npix, offset=0):
+        step = max(1, (W * H) // npix)
+        px = (np.arange(npix, dtype=np.uint64) * step + offset) % (W * H)
+        return (px[:, None] * spp + np.arange(spp, dtype=np.uint64)[None, :]).reshape(-1)
+
+    calib = ids_for(max(1, 512 // spp * 8), 7)
+    t0 = time.perf_counter()
+    o.render_paths(cam, opts, calib, threads=threads)
+    dt = time.perf_counter() - t0
+    rate = len(calib) / max(dt, 1e-6)
+    npix = int(max(16, min(W * H, rate * seconds / spp)))
+    ids = ids_for(npix, 13)
+    t0 = time.perf_counter()
+    o.render_paths(cam, opts, ids, threads=threads)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": len(ids) / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of %d pixels (stratified, every %dth) x %d spp = %d path samples in %.1f s"
+                      % (npix, W * H, max(1, (W * H) // npix), spp, len(ids), dt)}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from lambda_gb300 import abi, configs
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sb, cam, opts = configs.terrain(args.width, args.height, args.spp, 6)
+        K, W_ = args.steps, args.warmup
+        vals = []
+        for i in range(W_ + K):
+            cb = cpu_baseline(sb, cam, opts, max(2.0, min(args.cpu_seconds, 240.0 / (K + W_))))
+            if i >= W_:
+                vals.append(cb["value"])
+        v = float(np.median(vals))
+        cb["value"] = v
+        cfg = dict(WORKLOAD)
+        cfg["l2"] = "n/a (CPU)"
+        print(json.dumps({"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": K, "warmup": W_,
+                          "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f32", "data": "synthetic (seeded procedural scene)", "config": cfg,
+                          "impl": "reference", "cpu_baseline": cb,
+                          "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+
+    import torch
+    import lambda_gb300 as lg
+    lg.build()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    sb, cam, opts = configs.terrain(args.width, args.height, args.spp, 6)
+    opts.seed = 1 + rank
+    r = lg.Renderer(sb, device=dev)
+    W, H, spp = opts.width, opts.height, opts.spp
+    paths = W * H * spp
+    film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    # counting launch (outside the timed region): nodes / triangles / rays of one frame
+    stats = r.render_count(cam, opts)
+    for _ in range(args.warmup):
+        r.render_device(cam, opts, film.data_ptr(), stream=stream)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record()
+        r.render_device(cam, opts, film.data_ptr(), stream=stream)
+        ev[k][1].record()
+    t_end.record()
+    torch.cuda.synchronize()
+    total_ms = t_start.elapsed_time(t_end)
+    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    # end to end through the host-buffer API (film copies inside the timed region)
+    host_film = np.zeros((H, W, 4), np.float32)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        r.render(cam, opts, host_film)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([total_ms, e2e_s * 1e3], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_ms = float(t[0]), float(t[1])
+        dist.barrier()
+    else:
+        e2e_ms = e2e_s * 1e3
+    value = paths * args.steps * world / (total_ms / 1e3) / 1e6
+    e2e = paths * args.steps * world / (e2e_ms / 1e3) / 1e6
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    pk = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    node_b, tri_b = stats["node_bytes"], stats["tri_record_bytes"]
+    alg_bytes = stats["nodes_visited"] * node_b + stats["tris_tested"] * tri_b + paths * 16
+    mean_kernel_s = float(np.mean(kernel_ms)) / 1e3
+    achieved = alg_bytes / mean_kernel_s / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": NCU_TRAFFIC_PER_LAUNCH,
+            "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
+            "algorithmic_bytes_per_launch": alg_bytes, "nodes_visited": stats["nodes_visited"],
+            "tris_tested": stats["tris_tested"], "rays": stats["rays"],
+            "mrays_per_s": stats["rays"] / mean_kernel_s / 1e6, "kernel_ms": float(np.mean(kernel_ms))}
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(sb, cam, opts, args.cpu_seconds)
+    cfg = dict(WORKLOAD)
+    cfg["l2"] = "scene data > L2 and a 256 MiB buffer is written between timed steps"
+    cfg["width"], cfg["height"], cfg["spp"] = W, H, spp
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": cfg, "parallelism": "replicas" if world > 1 else "single GPU",
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": W * H * 16, "d2h_bytes_per_step": W * H * 16},
+            "gpu_launches": args.steps, "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
+    print(json.dumps(line))
+    r.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

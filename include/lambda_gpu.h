@@ -1,0 +1,325 @@
+/*
+ * lambda_gpu.h -- C ABI of the GB300 (sm_103a) MIS volumetric path-tracing module.
+ *
+ * The module replaces the per-sample CPU call chain of the Lambda renderer
+ *   TileRenderers::UniformSpp (src/render/Render.cpp:43-64)
+ *     -> MISVolumetricPathIntegrator::Li (src/integrators/MISVolumetricPathIntegrator.cpp:71-215)
+ *       -> Scene::Intersect / IntersectTr / MutualVisibility (src/core/Scene.cpp:28-107, Embree rtcIntersect1/rtcOccluded1)
+ *       -> Light / LightSampler / BxDF / Medium / shader-graph sockets
+ * with one call that renders a whole film on the GPU.  A GPU integrator needs every path of a
+ * frame at once, so the seam is frame granularity: the inputs are exactly the fields of
+ * lambda::RenderDirective {film, scene, camera, integrator, sampler, spp} (src/render/Render.h:12-20).
+ *
+ * The scene is handed over as flat, caller-owned arrays that mirror Lambda's object model:
+ *   meshes     <- TriangleMesh buffers        (src/core/TriangleMesh.h:13-83, include/lambda/Lambda.h:67-78)
+ *   objects    <- Scene::objects / Instance   (src/core/Scene.h:31, src/core/Instance.h)
+ *   materials  <- Material{bxdf, light, mediaBoundary} (src/shading/Material.h:18-32)
+ *   nodes      <- ShaderGraph::Node graph     (src/shading/graph/ShaderGraph.h:254-327, include/lambda/Material.h:245-290)
+ *   lights     <- Scene::lights               (src/lighting/)
+ *   media      <- HomogeneousMedium + HenyeyGreenstein (src/shading/media/)
+ * The module copies everything into device memory during lgpu_scene_commit and keeps no host
+ * pointer past the call (Lambda's TriangleMesh::AssignData aliases caller arrays instead).
+ *
+ * Error convention: every entry point returns an lgpu_status; lgpu_last_error() gives a message.
+ * No C++ exception crosses this boundary.  Calls on one context must be serialised by the caller.
+ */
+#ifndef LAMBDA_GPU_H
+#define LAMBDA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define LGPU_API __declspec(dllexport)
+#else
+#define LGPU_API __attribute__((visibility("default")))
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+typedef enum lgpu_status {
+    LGPU_OK = 0,
+    LGPU_ERR_INVALID_ARG = 1,
+    LGPU_ERR_CUDA = 2,
+    LGPU_ERR_OOM = 3,
+    LGPU_ERR_INVALID_SCENE = 4,
+    LGPU_ERR_UNSUPPORTED_NODE = 5,
+    LGPU_ERR_QUEUE_OVERFLOW = 6,
+    LGPU_ERR_TIMEOUT = 7,
+    LGPU_ERR_NO_SCENE = 8
+} lgpu_status;
+
+/* ---------------------------------------------------------------- enums mirrored from Lambda */
+
+/* Integrators.  Values 0-5 are include/lambda/Lambda.h:106-113 (LAMBDA_Integrator); the GPU
+ * MIS volumetric path integrator is the added value, the drop-in for
+ * MISVolumetricPathIntegrator (src/integrators/MISVolumetricPathIntegrator.h:9-22). */
+typedef enum lgpu_integrator {
+    LGPU_INTEGRATOR_PATH = 0,
+    LGPU_INTEGRATOR_VOLPATH = 1,
+    LGPU_INTEGRATOR_DIRECT = 2,
+    LGPU_INTEGRATOR_NORMAL = 3,
+    LGPU_INTEGRATOR_DEPTH = 4,
+    LGPU_INTEGRATOR_AOV = 5,
+    LGPU_INTEGRATOR_GPU_MISVOLPATH = 6
+} lgpu_integrator;
+
+/* include/lambda/Lambda.h:115-118 */
+typedef enum lgpu_light_strategy {
+    LGPU_LIGHT_STRATEGY_POWER = 0,   /* PowerLightSampler  src/lighting/LightSampler.cpp:14-35 */
+    LGPU_LIGHT_STRATEGY_TREE = 1     /* ManyLightSampler   src/lighting/ManyLightSampler.cpp */
+} lgpu_light_strategy;
+
+/* include/lambda/Material.h:232-237 */
+typedef enum lgpu_light_type {
+    LGPU_LIGHT_POINT = 0,
+    LGPU_LIGHT_MESH = 1,
+    LGPU_LIGHT_ENVIRONMENT = 2,
+    LGPU_LIGHT_SPOT = 3
+} lgpu_light_type;
+
+/* Shader node types: same values as LAMBDA_ShaderNodeType, include/lambda/Material.h:245-278. */
+typedef enum lgpu_node_type {
+    LGPU_NODE_BXDF_MIX = 0,
+    LGPU_NODE_BXDF_LAMBERTIAN = 1,
+    LGPU_NODE_BXDF_OREN_NAYAR_R = 2,
+    LGPU_NODE_BXDF_OREN_NAYAR_T = 3,
+    LGPU_NODE_BXDF_MICROFACET_R = 4,
+    LGPU_NODE_BXDF_MICROFACET_T = 5,   /* no reference implementation: rejected */
+    LGPU_NODE_BXDF_GHOST = 6,
+    LGPU_NODE_BXDF_FRESNEL = 7,
+    LGPU_NODE_BXDF_SPECULAR_R = 8,
+    LGPU_NODE_BXDF_SPECULAR_T = 9,
+    LGPU_NODE_SEPARATE_XYZ = 10,
+    LGPU_NODE_SEPARATE_RGBA = 11,
+    LGPU_NODE_MERGE_XYZ = 12,
+    LGPU_NODE_MERGE_RGBA = 13,
+    LGPU_NODE_SCALAR = 14,
+    LGPU_NODE_VECTOR3 = 15,
+    LGPU_NODE_VECTOR2 = 16,
+    LGPU_NODE_RGB = 17,
+    LGPU_NODE_SPECTRUM = 18,
+    LGPU_NODE_BLACKBODY = 19,
+    LGPU_NODE_IMAGE_TEXTURE = 20,
+    LGPU_NODE_SURFACE_INFO = 21,
+    LGPU_NODE_MATHS = 22,
+    LGPU_NODE_VECTOR_MATHS = 23,
+    LGPU_NODE_DOT_PRODUCT = 24,
+    LGPU_NODE_CROSS_PRODUCT = 25,
+    LGPU_NODE_VECTOR_MAGNITUDE = 26,
+    LGPU_NODE_PERLIN_NOISE = 27,
+    LGPU_NODE_VALUE_NOISE = 28,
+    LGPU_NODE_OCTAVE_NOISE = 29,
+    LGPU_NODE_CHECKER = 30,
+    LGPU_NODE_VORONOI = 31,
+    LGPU_NODE_TYPE_COUNT = 32
+} lgpu_node_type;
+
+/* ScalarOperatorType / VectorOperatorType, src/shading/graph/GraphMaths.h:9-16 */
+typedef enum lgpu_maths_op {
+    LGPU_MATHS_ADD = 0, LGPU_MATHS_SUBTRACT = 1, LGPU_MATHS_MULTIPLY = 2,
+    LGPU_MATHS_DIVIDE = 3, LGPU_MATHS_SQRT = 4, LGPU_MATHS_POWER = 5
+} lgpu_maths_op;
+
+/* Microfacet distributions, src/shading/MicrofacetDistribution.h:29-53 */
+typedef enum lgpu_distribution { LGPU_DIST_TROWBRIDGE_REITZ = 0, LGPU_DIST_BECKMANN = 1 } lgpu_distribution;
+
+/* Spectral representation.  RGB3 is the reference's `typedef RGBSpectrum Spectrum`
+ * (src/core/Spectrum.h:24).  HERO4 carries 4 hero wavelengths per path over 380-720 nm. */
+typedef enum lgpu_spectral_mode { LGPU_SPECTRAL_RGB3 = 0, LGPU_SPECTRAL_HERO4 = 1 } lgpu_spectral_mode;
+
+/* ---------------------------------------------------------------- scene description */
+
+/* TriangleMesh buffers (src/core/TriangleMesh.h:15-22).  Vertices are world space for plain mesh
+ * objects and object space for meshes used through instances. */
+typedef struct lgpu_mesh_desc {
+    const float *vertices;      /* 3 * num_vertices */
+    const uint32_t *triangles;  /* 3 * num_triangles (v0, v1, v2) */
+    const float *normals;       /* optional, 3 * num_vertices; enables smooth shading frames */
+    const float *tangents;      /* optional, 4 * num_vertices (xyz + handedness), needed with normals */
+    const float *uvs;           /* optional, 2 * num_vertices */
+    uint32_t num_vertices;
+    uint32_t num_triangles;
+} lgpu_mesh_desc;
+
+/* One entry of Scene::objects.  kind 0 = the mesh itself (TriangleMesh object), kind 1 = an
+ * Instance of the mesh used as an InstanceProxy, placed by a column-major 3x3 + translation
+ * affine (affine3<Real>::xfm layout, src/maths/affine3.h:18-30). */
+typedef struct lgpu_object_desc {
+    int32_t mesh;
+    int32_t kind;
+    int32_t material;
+    int32_t pad;
+    float xfm[12];
+} lgpu_object_desc;
+
+/* Material{bxdf, light, mediaBoundary} (src/shading/Material.h:18-24).  bxdf_node = -1 is a
+ * null surface (a pure media boundary, skipped by IntersectTr).  light = index into lights or -1. */
+typedef struct lgpu_material_desc {
+    int32_t bxdf_node;
+    int32_t light;
+    int32_t medium_interior;
+    int32_t medium_exterior;
+} lgpu_material_desc;
+
+#define LGPU_NODE_MAX_INPUTS 4
+
+/* One shader node.  Input i is linked to output socket in_socket[i] of node in_node[i] when
+ * in_node[i] >= 0, else it reads its SocketRef default value in_default[i] (SocketRef::data,
+ * ShaderGraph.h:254-284).  params hold the node's own constants:
+ *   SCALAR: value | VECTOR2/VECTOR3/RGB: components | SPECTRUM: rgb of a constant spectrum
+ *   BLACKBODY: samples | PERLIN/VALUE/CHECKER/VORONOI: scale | OCTAVE: scale, octaves
+ *   MICROFACET_R: distribution, fresnel etaT | SPECULAR_R: fresnel etaT | SPECULAR_T: etaT
+ * op: lgpu_maths_op for MATHS / VECTOR_MATHS.
+ * OCTAVE_NOISE takes its inner noise node (Octave::noise) as in_node[0]. */
+typedef struct lgpu_node_desc {
+    int32_t type;
+    int32_t op;
+    float params[4];
+    int32_t in_node[LGPU_NODE_MAX_INPUTS];
+    int32_t in_socket[LGPU_NODE_MAX_INPUTS];
+    float in_default[LGPU_NODE_MAX_INPUTS][4];
+} lgpu_node_desc;
+
+/* Lights (src/lighting/).  MESH: object = emitting object, emission = node/socket
+ * (MeshLight::emission), intensity.  POINT/SPOT: position, axis, cone/falloff angles in radians,
+ * emission socket, intensity.  ENVIRONMENT: RGB float texture env_width x env_height, scanline
+ * rows, equirectangular (EnvironmentLight.cpp:7-22), intensity and offset. */
+typedef struct lgpu_light_desc {
+    int32_t type;
+    int32_t object;
+    int32_t emission_node;
+    int32_t emission_socket;
+    float intensity;
+    float position[3];
+    float axis[3];
+    float cone_angle;
+    float falloff_start;
+    float offset[2];
+    int32_t env_width;
+    int32_t env_height;
+    int32_t pad;
+    const float *env_texture;
+} lgpu_light_desc;
+
+/* HomogeneousMedium(sigmaA, sigmaS) + HenyeyGreenstein(g) (src/shading/media/HomogeneousMedium.h). */
+typedef struct lgpu_medium_desc {
+    float sigma_a[3];
+    float sigma_s[3];
+    float g;
+    float pad;
+} lgpu_medium_desc;
+
+typedef struct lgpu_scene_desc {
+    const lgpu_mesh_desc *meshes;       int32_t num_meshes;
+    const lgpu_object_desc *objects;    int32_t num_objects;
+    const lgpu_material_desc *materials; int32_t num_materials;
+    const lgpu_node_desc *nodes;        int32_t num_nodes;
+    const lgpu_light_desc *lights;      int32_t num_lights;
+    const lgpu_medium_desc *media;      int32_t num_media;
+    int32_t has_volumes;      /* Scene::hasVolumes (src/core/Scene.h:36) */
+    int32_t light_strategy;   /* lgpu_light_strategy */
+} lgpu_scene_desc;
+
+/* Pinhole camera (src/camera/Camera.cpp:7-44): origin, the three axes and the field of view.
+ * aspect = height / width as in Camera::Camera. */
+typedef struct lgpu_camera_desc {
+    float origin[3];
+    float x_hat[3];
+    float y_hat[3];
+    float z_hat[3];
+    float fov;
+    int32_t type;             /* 0 = pinhole */
+} lgpu_camera_desc;
+
+/* RenderDirective fields (src/render/Render.h:12-20) plus the GPU-side knobs. */
+typedef struct lgpu_render_opts {
+    int32_t width;
+    int32_t height;
+    int32_t spp;
+    int32_t max_bounces;      /* MISVolumetricPathIntegrator::maxBounces */
+    int32_t min_bounces;      /* MISVolumetricPathIntegrator::minBounces (Russian roulette start) */
+    int32_t integrator;       /* lgpu_integrator */
+    int32_t spectral_mode;    /* lgpu_spectral_mode */
+    uint32_t seed;            /* counter-based RNG key */
+    uint32_t sample_offset;   /* first sample index: resume = same seed, offset = samples done */
+    int32_t block_size;       /* 0 = autotuned default */
+} lgpu_render_opts;
+
+/* Per-render statistics.  Traversal counters are filled only by lgpu_render_count. */
+typedef struct lgpu_stats {
+    double last_render_ms;
+    uint64_t paths;
+    uint64_t rays;            /* closest-hit + occlusion queries issued */
+    uint64_t nodes_visited;   /* BVH node fetches over all queries */
+    uint64_t tris_tested;     /* triangle records fetched over all queries */
+    uint64_t bvh_nodes;
+    uint64_t bvh_bytes;
+    uint64_t tri_bytes;
+    uint32_t node_bytes;      /* size of one BVH node record */
+    uint32_t tri_record_bytes;/* size of one triangle record */
+    uint64_t device_bytes;    /* device memory held by the committed scene */
+} lgpu_stats;
+
+typedef struct lgpu_context lgpu_context;
+
+/* Create a context on CUDA device `device`.  Replaces lambdaCreateDevice
+ * (include/lambda/Lambda.h:37) for the GPU path. */
+LGPU_API int lgpu_create(lgpu_context **out, int device);
+
+/* Free the context and every device buffer it owns (lambdaReleaseDevice, Lambda.h:40). */
+LGPU_API void lgpu_destroy(lgpu_context *ctx);
+
+/* Message of the last failed call on ctx (never NULL). */
+LGPU_API const char *lgpu_last_error(const lgpu_context *ctx);
+
+/* Compile and upload a scene: BVH build, light-tree build, shader-graph bytecode.
+ * Replaces Scene::AddObject + Scene::Commit (src/core/Scene.cpp:18-26, 114-121) and
+ * LightSampler::Commit (ManyLightSampler.cpp:37-44). */
+LGPU_API int lgpu_scene_commit(lgpu_context *ctx, const lgpu_scene_desc *scene);
+
+/* Render `opts->spp` samples per pixel and ADD them to the host film `film_rgbn`
+ * (width*height float4: summed RGB + sample count), the way Film::AddSample accumulates
+ * (src/camera/Film.h:30-33).  Host buffers: the call copies the film to and from the device.
+ * Replaces MosaicRenderer::Render over TileRenderers::UniformSpp (src/render/Render.cpp:43-64). */
+LGPU_API int lgpu_render(lgpu_context *ctx, const lgpu_camera_desc *camera,
+                         const lgpu_render_opts *opts, float *film_rgbn);
+
+/* Same, on device memory: film_rgbn_dev is a device float4 film that the render adds into;
+ * path_out_dev (optional, may be NULL) receives the radiance of every path, indexed
+ * (y * width + x) * spp + s, as float4.  stream = cudaStream_t or NULL. */
+LGPU_API int lgpu_render_device(lgpu_context *ctx, const lgpu_camera_desc *camera,
+                                const lgpu_render_opts *opts, float *film_rgbn_dev,
+                                float *path_out_dev, void *stream);
+
+/* Render a chosen list of paths (path index = (y * width + x) * spp + s) and write their
+ * radiance to path_out_host (n * 4 floats).  Used for per-path parity checks. */
+LGPU_API int lgpu_render_paths(lgpu_context *ctx, const lgpu_camera_desc *camera,
+                               const lgpu_render_opts *opts, const uint64_t *path_ids,
+                               uint64_t n, float *path_out_host);
+
+/* Render once with in-kernel traversal counters on (nodes, triangles, rays); the counts land in
+ * lgpu_get_stats.  The film is not touched. */
+LGPU_API int lgpu_render_count(lgpu_context *ctx, const lgpu_camera_desc *camera,
+                               const lgpu_render_opts *opts);
+
+/* Closest-hit queries for a batch of rays (Scene::Intersect, src/core/Scene.cpp:28-43).
+ * rays: n * 8 floats (ox, oy, oz, tnear, dx, dy, dz, tfar), device pointer.  hits: n * 4 words
+ * (t as float bits, primId, objectId, instance-or-~0), device pointer.  u, v are written to
+ * uv_out (n * 2 floats, device, optional). */
+LGPU_API int lgpu_intersect(lgpu_context *ctx, const float *rays_dev, uint32_t *hits_dev,
+                            float *uv_out_dev, uint64_t n, void *stream);
+
+LGPU_API int lgpu_get_stats(const lgpu_context *ctx, lgpu_stats *out);
+
+/* Version string of the module. */
+LGPU_API const char *lgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LAMBDA_GPU_H */

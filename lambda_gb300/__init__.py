@@ -1,0 +1,130 @@
+"""lambda_gb300: GB300-native (sm_103a) MIS volumetric path tracer behind Lambda's scene API.
+
+The compute path is the CUDA library lambda_gb300/_build/liblambda_gpu.so (C ABI declared in
+include/lambda_gpu.h); this module only binds it with ctypes.  There is no CPU fallback: if the
+library or a GPU is missing, every entry point raises.
+"""
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+from . import abi
+from .scene import Camera, SceneBuilder, out  # noqa: F401
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liblambda_gpu.so"
+
+EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_scene_commit", "lgpu_render",
+           "lgpu_render_device", "lgpu_render_paths", "lgpu_render_count", "lgpu_intersect",
+           "lgpu_get_stats", "lgpu_version"]
+
+_lib = None
+
+
+class LambdaGPUError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("lgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+def build(force=False):
+    from .build import build as _b
+    return _b(force=force)
+
+
+def lib():
+    """Load the CUDA extension; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError("CUDA extension %s is missing: run lambda_gb300.build()" % LIB_PATH)
+        L = C.CDLL(str(LIB_PATH))
+        vp = C.c_void_p
+        L.lgpu_create.argtypes = [C.POINTER(vp), C.c_int]
+        L.lgpu_destroy.argtypes = [vp]
+        L.lgpu_destroy.restype = None
+        L.lgpu_last_error.argtypes = [vp]
+        L.lgpu_last_error.restype = C.c_char_p
+        L.lgpu_scene_commit.argtypes = [vp, C.POINTER(abi.SceneDesc)]
+        L.lgpu_render.argtypes = [vp, C.POINTER(abi.CameraDesc), C.POINTER(abi.RenderOpts), vp]
+        L.lgpu_render_device.argtypes = [vp, C.POINTER(abi.CameraDesc), C.POINTER(abi.RenderOpts), vp, vp, vp]
+        L.lgpu_render_paths.argtypes = [vp, C.POINTER(abi.CameraDesc), C.POINTER(abi.RenderOpts), vp, C.c_uint64, vp]
+        L.lgpu_render_count.argtypes = [vp, C.POINTER(abi.CameraDesc), C.POINTER(abi.RenderOpts)]
+        L.lgpu_intersect.argtypes = [vp, vp, vp, vp, C.c_uint64, vp]
+        L.lgpu_get_stats.argtypes = [vp, C.POINTER(abi.Stats)]
+        L.lgpu_version.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Renderer:
+    """One GPU context holding one committed scene (lgpu_create + lgpu_scene_commit)."""
+
+    def __init__(self, scene, device=0):
+        L = lib()
+        h = C.c_void_p()
+        rc = L.lgpu_create(C.byref(h), device)
+        if rc != 0:
+            raise LambdaGPUError(rc, "lgpu_create failed (no CUDA device?)")
+        self._h = h
+        self._desc = scene.desc()
+        self._scene = scene
+        self._check(L.lgpu_scene_commit(self._h, C.byref(self._desc)))
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LambdaGPUError(rc, lib().lgpu_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().lgpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def render(self, camera, opts, film=None):
+        """Host-buffer render (lgpu_render): adds opts.spp samples into film (H, W, 4)."""
+        if film is None:
+            film = np.zeros((opts.height, opts.width, 4), np.float32)
+        cam = camera.desc()
+        self._check(lib().lgpu_render(self._h, C.byref(cam), C.byref(opts), _ptr(film)))
+        return film
+
+    def render_device(self, camera, opts, film_ptr, paths_ptr=None, stream=None):
+        """Device-buffer render: film_ptr / paths_ptr are device addresses (ints)."""
+        cam = camera.desc()
+        self._check(lib().lgpu_render_device(self._h, C.byref(cam), C.byref(opts), C.c_void_p(film_ptr),
+                                             C.c_void_p(paths_ptr) if paths_ptr else None,
+                                             C.c_void_p(stream) if stream else None))
+
+    def render_paths(self, camera, opts, path_ids):
+        ids = np.ascontiguousarray(path_ids, np.uint64)
+        outp = np.zeros((len(ids), 4), np.float32)
+        cam = camera.desc()
+        self._check(lib().lgpu_render_paths(self._h, C.byref(cam), C.byref(opts), _ptr(ids), len(ids), _ptr(outp)))
+        return outp
+
+    def render_count(self, camera, opts):
+        cam = camera.desc()
+        self._check(lib().lgpu_render_count(self._h, C.byref(cam), C.byref(opts)))
+        return self.stats()
+
+    def intersect(self, rays_ptr, hits_ptr, uv_ptr, n, stream=None):
+        self._check(lib().lgpu_intersect(self._h, C.c_void_p(rays_ptr), C.c_void_p(hits_ptr),
+                                         C.c_void_p(uv_ptr) if uv_ptr else None, n,
+                                         C.c_void_p(stream) if stream else None))
+
+    def stats(self):
+        s = abi.Stats()
+        self._check(lib().lgpu_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in abi.Stats._fields_}

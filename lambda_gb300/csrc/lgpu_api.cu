@@ -1,0 +1,752 @@
+/*
+ * C ABI of the GB300 path tracer (include/lambda_gpu.h): context, scene compilation and upload,
+ * render entry points.
+ *
+ * lgpu_scene_commit is the GPU counterpart of Scene::AddObject + Scene::Commit +
+ * LightSampler::Commit (src/core/Scene.cpp:18-26, 114-121; src/lighting/ManyLightSampler.cpp:37-44):
+ *   - every plain mesh object goes into one world BLAS (world-space triangles, object id per
+ *     triangle); every mesh used through instances gets one BLAS in object space (InstanceProxy);
+ *     a TLAS over instance records (world BLAS + each Instance with its world->object affine)
+ *     exists only when the scene has instances;
+ *   - materials and light emission sockets are compiled to bytecode;
+ *   - lights become a flat table plus triangle-area CDFs, a power CDF and the light tree.
+ * All buffers are copied into device memory; no caller pointer is kept.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lambda_gpu.h"
+#include "lgpu_build.h"
+#include "lgpu_device.cuh"
+#include "lgpu_launch.h"
+#include "lgpu_lighttree.h"
+
+using namespace lg;
+
+struct lgpu_context {
+    int device = 0;
+    std::string err;
+    std::vector<void *> scene_allocs;
+    DeviceScene S;
+    bool have_scene = false;
+    lgpu_stats stats;
+    unsigned long long *d_counters = nullptr;
+    float4 *d_film = nullptr;
+    size_t film_px = 0;
+    float4 *d_paths = nullptr;
+    size_t paths_cap = 0;
+    uint64_t *d_ids = nullptr;
+    size_t ids_cap = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+int fail(lgpu_context *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+int cuda_fail(lgpu_context *c, cudaError_t e, const char *what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? LGPU_ERR_OOM : LGPU_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void free_scene(lgpu_context *c) {
+    for (void *p : c->scene_allocs) cudaFree(p);
+    c->scene_allocs.clear();
+    c->have_scene = false;
+    std::memset(&c->S, 0, sizeof(c->S));
+}
+
+template <class T>
+bool upload(lgpu_context *c, const std::vector<T> &v, const T **dst, size_t &bytes) {
+    *dst = nullptr;
+    if (v.empty()) return true;
+    void *p = nullptr;
+    const size_t sz = v.size() * sizeof(T);
+    cudaError_t e = cudaMalloc(&p, sz);
+    if (e != cudaSuccess) { cuda_fail(c, e, "cudaMalloc"); return false; }
+    c->scene_allocs.push_back(p);
+    e = cudaMemcpy(p, v.data(), sz, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { cuda_fail(c, e, "cudaMemcpy"); return false; }
+    *dst = reinterpret_cast<const T *>(p);
+    bytes += sz;
+    return true;
+}
+
+void inverse3(const float *m, float *inv) {   /* column-major 3x3 inverse in double */
+    const double a = m[0], b = m[3], cc = m[6], d = m[1], e = m[4], f = m[7], g = m[2], h = m[5], i = m[8];
+    const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+    const double det = a * A + b * B + cc * C;
+    const double id = 1.0 / det;
+    const double r[9] = {A * id, -(b * i - cc * h) * id, (b * f - cc * e) * id,
+                         B * id, (a * i - cc * g) * id, -(a * f - cc * d) * id,
+                         C * id, -(a * h - b * g) * id, (a * e - b * d) * id};
+    inv[0] = (float)r[0]; inv[3] = (float)r[1]; inv[6] = (float)r[2];
+    inv[1] = (float)r[3]; inv[4] = (float)r[4]; inv[7] = (float)r[5];
+    inv[2] = (float)r[6]; inv[5] = (float)r[7]; inv[8] = (float)r[8];
+}
+
+inline lt::V3f v3(const float *p) { lt::V3f r; r.x = p[0]; r.y = p[1]; r.z = p[2]; return r; }
+
+}  // namespace
+
+extern "C" {
+
+LGPU_API const char *lgpu_version(void) { return "lambda-gb300 0.1 (sm_103a, BVH2 megakernel)"; }
+
+LGPU_API int lgpu_create(lgpu_context **out, int device) {
+    if (!out) return LGPU_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return LGPU_ERR_CUDA;
+    if (device < 0 || device >= n) return LGPU_ERR_INVALID_ARG;
+    lgpu_context *c = new lgpu_context();
+    c->device = device;
+    std::memset(&c->stats, 0, sizeof(c->stats));
+    std::memset(&c->S, 0, sizeof(c->S));
+    e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e != cudaSuccess) { delete c; return LGPU_ERR_CUDA; }
+    *out = c;
+    return LGPU_OK;
+}
+
+LGPU_API void lgpu_destroy(lgpu_context *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    free_scene(c);
+    cudaFree(c->d_counters);
+    cudaFree(c->d_film);
+    cudaFree(c->d_paths);
+    cudaFree(c->d_ids);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    delete c;
+}
+
+LGPU_API const char *lgpu_last_error(const lgpu_context *c) { return c ? c->err.c_str() : "null context"; }
+
+LGPU_API int lgpu_get_stats(const lgpu_context *c, lgpu_stats *out) {
+    if (!c || !out) return LGPU_ERR_INVALID_ARG;
+    *out = c->stats;
+    return LGPU_OK;
+}
+
+LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
+    if (!c || !d) return LGPU_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    free_scene(c);
+    /* ---------------- validation */
+    for (int i = 0; i < d->num_objects; ++i) {
+        const lgpu_object_desc &o = d->objects[i];
+        if (o.mesh < 0 || o.mesh >= d->num_meshes) return fail(c, LGPU_ERR_INVALID_SCENE, "object " + std::to_string(i) + " has no mesh");
+        if (o.material < 0 || o.material >= d->num_materials) return fail(c, LGPU_ERR_INVALID_SCENE, "object " + std::to_string(i) + " has no material");
+    }
+    for (int i = 0; i < d->num_meshes; ++i) {
+        const lgpu_mesh_desc &m = d->meshes[i];
+        for (uint32_t t = 0; t < 3 * m.num_triangles; ++t)
+            if (m.triangles[t] >= m.num_vertices) return fail(c, LGPU_ERR_INVALID_SCENE, "mesh " + std::to_string(i) + " indexes a missing vertex");
+    }
+    if (d->num_lights == 0) return fail(c, LGPU_ERR_INVALID_SCENE, "scene has no light (the reference requires one)");
+
+    std::vector<float> fpool;
+    DeviceScene S;
+    std::memset(&S, 0, sizeof(S));
+    S.has_volumes = d->has_volumes;
+    S.light_strategy = d->light_strategy;
+    S.num_lights = d->num_lights;
+    size_t bytes = 0;
+
+    /* ---------------- meshes: vertex attributes */
+    std::vector<float4> pos, nrm, tan;
+    std::vector<float2> uv;
+    std::vector<uint4> tri_idx;
+    std::vector<DMesh> meshes(d->num_meshes);
+    for (int i = 0; i < d->num_meshes; ++i) {
+        const lgpu_mesh_desc &m = d->meshes[i];
+        DMesh &dm = meshes[i];
+        dm.vtx_off = (int)pos.size();
+        dm.tri_off = (int)tri_idx.size();
+        dm.num_tris = (int)m.num_triangles;
+        dm.flags = ((m.normals && m.tangents) ? 1 : 0) | (m.uvs ? 2 : 0);
+        for (uint32_t v = 0; v < m.num_vertices; ++v) {
+            pos.push_back(make_float4(m.vertices[3 * v], m.vertices[3 * v + 1], m.vertices[3 * v + 2], 0.f));
+            nrm.push_back((dm.flags & 1) ? make_float4(m.normals[3 * v], m.normals[3 * v + 1], m.normals[3 * v + 2], 0.f) : make_float4(0, 0, 0, 0));
+            tan.push_back((dm.flags & 1) ? make_float4(m.tangents[4 * v], m.tangents[4 * v + 1], m.tangents[4 * v + 2], m.tangents[4 * v + 3]) : make_float4(0, 0, 0, 0));
+            uv.push_back(m.uvs ? make_float2(m.uvs[2 * v], m.uvs[2 * v + 1]) : make_float2(0, 0));
+        }
+        for (uint32_t t = 0; t < m.num_triangles; ++t)
+            tri_idx.push_back(make_uint4(m.triangles[3 * t], m.triangles[3 * t + 1], m.triangles[3 * t + 2], 0u));
+    }
+
+    /* ---------------- objects */
+    std::vector<DObject> objects(d->num_objects);
+    lt::Box sceneBox;
+    bool firstBox = true;
+    std::vector<lt::Box> objBox(d->num_objects);
+    for (int i = 0; i < d->num_objects; ++i) {
+        const lgpu_object_desc &o = d->objects[i];
+        DObject &ob = objects[i];
+        ob.mesh = o.mesh; ob.material = o.material; ob.kind = o.kind;
+        static const float id12[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+        const float *x = o.kind == 1 ? o.xfm : id12;
+        for (int k = 0; k < 9; ++k) ob.m[k] = x[k];
+        for (int k = 0; k < 3; ++k) ob.t[k] = x[9 + k];
+        ob.identity = 1;
+        for (int k = 0; k < 12; ++k) if (x[k] != id12[k]) ob.identity = 0;
+        float inv[9];
+        inverse3(ob.m, inv);
+        for (int r = 0; r < 3; ++r) for (int cidx = 0; cidx < 3; ++cidx) ob.nrm[cidx * 3 + r] = inv[r * 3 + cidx];
+        /* world bounds from transformed vertices, as the oracle computes them */
+        const lgpu_mesh_desc &m = d->meshes[o.mesh];
+        lt::Box b;
+        for (uint32_t v = 0; v < m.num_vertices; ++v) {
+            const float *p = m.vertices + 3 * v;
+            lt::V3f w;
+            if (ob.identity) w = v3(p);
+            else {
+                w.x = ob.m[0] * p[0] + ob.m[3] * p[1] + ob.m[6] * p[2];
+                w.y = ob.m[1] * p[0] + ob.m[4] * p[1] + ob.m[7] * p[2];
+                w.z = ob.m[2] * p[0] + ob.m[5] * p[1] + ob.m[8] * p[2];
+                w.x = w.x + ob.t[0]; w.y = w.y + ob.t[1]; w.z = w.z + ob.t[2];
+            }
+            lt::Box pb; pb.mn = w; pb.mx = w;
+            b = v == 0 ? pb : lt::Box::unite(b, pb);
+        }
+        objBox[i] = b;
+        sceneBox = firstBox ? b : lt::Box::unite(sceneBox, b);
+        firstBox = false;
+    }
+
+    /* ---------------- geometry: BLAS / TLAS */
+    std::vector<DNode> nodes;
+    std::vector<DTri> tris;
+    std::vector<DInst> insts;
+    auto make_tri = [&](const lgpu_mesh_desc &m, uint32_t t, int objId) {
+        const float *v0 = m.vertices + 3 * m.triangles[3 * t], *v1 = m.vertices + 3 * m.triangles[3 * t + 1], *v2 = m.vertices + 3 * m.triangles[3 * t + 2];
+        DTri T;
+        T.v0 = make_float4(v0[0], v0[1], v0[2], bits_to_float((int)t));
+        T.e1 = make_float4(v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2], bits_to_float(objId));
+        T.e2 = make_float4(v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2], 0.f);
+        return T;
+    };
+    auto tri_box = [&](const lgpu_mesh_desc &m, uint32_t t) {
+        Aabb b;
+        for (int k = 0; k < 3; ++k) { b.lo[k] = INFINITY; b.hi[k] = -INFINITY; }
+        for (int j = 0; j < 3; ++j) {
+            const float *p = m.vertices + 3 * m.triangles[3 * t + j];
+            for (int k = 0; k < 3; ++k) { b.lo[k] = std::min(b.lo[k], p[k]); b.hi[k] = std::max(b.hi[k], p[k]); }
+        }
+        return b;
+    };
+    int maxDepth = 0;
+    /* world BLAS over plain mesh objects */
+    std::vector<std::pair<int, uint32_t>> worldPrims;   /* (object, triangle) */
+    bool anyInstance = false;
+    for (int i = 0; i < d->num_objects; ++i) {
+        if (d->objects[i].kind == 1) { anyInstance = true; continue; }
+        const lgpu_mesh_desc &m = d->meshes[d->objects[i].mesh];
+        for (uint32_t t = 0; t < m.num_triangles; ++t) worldPrims.push_back({i, t});
+    }
+    int worldRoot;
+    {
+        std::vector<Aabb> boxes(worldPrims.size());
+        for (size_t k = 0; k < worldPrims.size(); ++k) boxes[k] = tri_box(d->meshes[d->objects[worldPrims[k].first].mesh], worldPrims[k].second);
+        BvhOut bo;
+        build_bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo);
+        maxDepth = std::max(maxDepth, bo.max_depth);
+        nodes.insert(nodes.end(), bo.nodes.begin(), bo.nodes.end());
+        for (uint32_t k : bo.order) {
+            const auto &wp = worldPrims[k];
+            tris.push_back(make_tri(d->meshes[d->objects[wp.first].mesh], wp.second, wp.first));
+        }
+        worldRoot = bo.root_ref;
+    }
+    if (anyInstance) {
+        std::vector<int> blasRoot(d->num_meshes, -1);
+        std::vector<Aabb> instBoxes;
+        if (!worldPrims.empty()) {
+            DInst I;
+            I.r0 = make_float4(1, 0, 0, 0); I.r1 = make_float4(0, 1, 0, 0); I.r2 = make_float4(0, 0, 1, 0);
+            I.root = worldRoot; I.object = -1; I.pad0 = I.pad1 = 0;
+            insts.push_back(I);
+            Aabb wb;
+            for (int k = 0; k < 3; ++k) { wb.lo[k] = INFINITY; wb.hi[k] = -INFINITY; }
+            for (int i = 0; i < d->num_objects; ++i) {
+                if (d->objects[i].kind == 1) continue;
+                const lt::Box &b = objBox[i];
+                wb.lo[0] = std::min(wb.lo[0], b.mn.x); wb.lo[1] = std::min(wb.lo[1], b.mn.y); wb.lo[2] = std::min(wb.lo[2], b.mn.z);
+                wb.hi[0] = std::max(wb.hi[0], b.mx.x); wb.hi[1] = std::max(wb.hi[1], b.mx.y); wb.hi[2] = std::max(wb.hi[2], b.mx.z);
+            }
+            instBoxes.push_back(wb);
+        }
+        for (int i = 0; i < d->num_objects; ++i) {
+            const lgpu_object_desc &o = d->objects[i];
+            if (o.kind != 1) continue;
+            if (blasRoot[o.mesh] < 0) {
+                const lgpu_mesh_desc &m = d->meshes[o.mesh];
+                std::vector<Aabb> boxes(m.num_triangles);
+                for (uint32_t t = 0; t < m.num_triangles; ++t) boxes[t] = tri_box(m, t);
+                BvhOut bo;
+                build_bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo);
+                maxDepth = std::max(maxDepth, bo.max_depth);
+                nodes.insert(nodes.end(), bo.nodes.begin(), bo.nodes.end());
+                for (uint32_t k : bo.order) tris.push_back(make_tri(m, k, -1));
+                blasRoot[o.mesh] = bo.root_ref;
+            }
+            const DObject &ob = objects[i];
+            float inv[9];
+            inverse3(ob.m, inv);
+            /* world -> object: x_obj = inv * (x - t) */
+            const float tx = -(inv[0] * ob.t[0] + inv[3] * ob.t[1] + inv[6] * ob.t[2]);
+            const float ty = -(inv[1] * ob.t[0] + inv[4] * ob.t[1] + inv[7] * ob.t[2]);
+            const float tz = -(inv[2] * ob.t[0] + inv[5] * ob.t[1] + inv[8] * ob.t[2]);
+            DInst I;
+            I.r0 = make_float4(inv[0], inv[3], inv[6], tx);
+            I.r1 = make_float4(inv[1], inv[4], inv[7], ty);
+            I.r2 = make_float4(inv[2], inv[5], inv[8], tz);
+            I.root = blasRoot[o.mesh]; I.object = i; I.pad0 = I.pad1 = 0;
+            insts.push_back(I);
+            const lt::Box &b = objBox[i];
+            Aabb ab;
+            ab.lo[0] = b.mn.x; ab.lo[1] = b.mn.y; ab.lo[2] = b.mn.z;
+            ab.hi[0] = b.mx.x; ab.hi[1] = b.mx.y; ab.hi[2] = b.mx.z;
+            instBoxes.push_back(ab);
+        }
+        BvhOut bo;
+        build_bvh(instBoxes, 1, (int)nodes.size(), 0, bo);
+        nodes.insert(nodes.end(), bo.nodes.begin(), bo.nodes.end());
+        std::vector<DInst> reordered;
+        for (uint32_t k : bo.order) reordered.push_back(insts[k]);
+        insts.swap(reordered);
+        S.root = bo.root_ref;
+        S.use_tlas = 1;
+        maxDepth += bo.max_depth + 1;
+    } else {
+        S.root = worldRoot;
+        S.use_tlas = 0;
+    }
+    if (maxDepth > LGPU_STACK - 4) return fail(c, LGPU_ERR_INVALID_SCENE, "BVH too deep for the traversal stack");
+
+    /* ---------------- materials */
+    std::vector<DIns> code;
+    GraphCompiler gc;
+    gc.d = d;
+    gc.code = &code;
+    std::vector<DMaterial> mats(d->num_materials);
+    for (int i = 0; i < d->num_materials; ++i) {
+        const lgpu_material_desc &md = d->materials[i];
+        DMaterial &m = mats[i];
+        std::memset(&m, 0, sizeof(m));
+        m.light = md.light;
+        m.medium_interior = md.medium_interior;
+        m.medium_exterior = md.medium_exterior;
+        m.has_bsdf = md.bxdf_node >= 0;
+        m.prog_off = 0; m.prog_len = 0;
+        if (md.light >= d->num_lights) return fail(c, LGPU_ERR_INVALID_SCENE, "material light index out of range");
+        if (md.medium_interior >= d->num_media || md.medium_exterior >= d->num_media) return fail(c, LGPU_ERR_INVALID_SCENE, "material medium index out of range");
+        if (m.has_bsdf && !gc.compile_material(md.bxdf_node, m))
+            return fail(c, LGPU_ERR_UNSUPPORTED_NODE, "material " + std::to_string(i) + ": " + gc.err);
+    }
+
+    /* ---------------- lights */
+    std::vector<DLight> lights(d->num_lights);
+    std::vector<lt::TreeLightIn> treeIn;
+    std::vector<int2> treeRef;      /* (light, tri) per tree light, input order */
+    std::vector<int> lightSlot(d->num_lights, -1);
+    std::vector<float> lightPower(d->num_lights, 0.f);
+    int envLight = -1;
+    DEnv env;
+    std::memset(&env, 0, sizeof(env));
+    std::vector<float4> envTex;
+    const float PIf = 3.14159265358979323846f;
+    for (int i = 0; i < d->num_lights; ++i) {
+        const lgpu_light_desc &ld = d->lights[i];
+        DLight &L = lights[i];
+        std::memset(&L, 0, sizeof(L));
+        L.intensity = ld.intensity;
+        L.object = ld.object;
+        L.dist_off = -1;
+        L.tri_base = -1;
+        if (ld.type != LGPU_LIGHT_ENVIRONMENT) {
+            if (ld.emission_node < 0 || ld.emission_node >= d->num_nodes) return fail(c, LGPU_ERR_INVALID_SCENE, "light " + std::to_string(i) + " has no emission socket");
+            if (!gc.compile_emission(ld.emission_node, ld.emission_socket, L.prog_off, L.prog_len, L.out_reg))
+                return fail(c, LGPU_ERR_UNSUPPORTED_NODE, "light " + std::to_string(i) + ": " + gc.err);
+        }
+        if (ld.type == LGPU_LIGHT_MESH) {
+            if (ld.object < 0 || ld.object >= d->num_objects) return fail(c, LGPU_ERR_INVALID_SCENE, "mesh light without object");
+            L.type = LT_MESH;
+            const lgpu_mesh_desc &m = d->meshes[d->objects[ld.object].mesh];
+            std::vector<float> areas(m.num_triangles);
+            float meshArea = 0;
+            L.tri_base = (int)treeIn.size();
+            /* TriangleLight::Irradiance: emission luminance at 3x3 barycentric points (RGB semantics) */
+            for (uint32_t t = 0; t < m.num_triangles; ++t) {
+                const lt::V3f a = v3(m.vertices + 3 * m.triangles[3 * t]), b = v3(m.vertices + 3 * m.triangles[3 * t + 1]),
+                              cc = v3(m.vertices + 3 * m.triangles[3 * t + 2]);
+                const lt::V3f e1 = b - a, e2 = cc - a;
+                const lt::V3f cr = {e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+                const float crm = std::sqrt(cr.x * cr.x + cr.y * cr.y + cr.z * cr.z);
+                areas[t] = crm * .5f;
+                meshArea += crm;
+                float irr = 0.f;
+                const float inv3 = 1.f / 3.f;
+                for (unsigned aa = 0; aa < 3; ++aa)
+                    for (unsigned bb = 0; bb < 3; ++bb) {
+                        ShadeCtx sc;
+                        std::memset(&sc, 0, sizeof(sc));
+                        sc.eta = 1.001f;
+                        if (m.uvs) {
+                            const float *u0 = m.uvs + 2 * m.triangles[3 * t], *u1 = m.uvs + 2 * m.triangles[3 * t + 1], *u2 = m.uvs + 2 * m.triangles[3 * t + 2];
+                            const float fu = (float)aa * inv3, fv = (float)bb * inv3;
+                            sc.uv = make_float2(u0[0] + (u1[0] - u0[0]) * fu + (u2[0] - u0[0]) * fv, u0[1] + (u1[1] - u0[1]) * fu + (u2[1] - u0[1]) * fv);
+                        }
+                        float4 R[LGPU_MAX_REGS];
+                        Lambda4 lam;
+                        run_prog<3>(code.data() + L.prog_off, L.prog_len, sc, lam, R);
+                        irr += spec_y<3>(Spec<3>::from4(R[L.out_reg]), lam);
+                    }
+                const float irradiance = irr * inv3 * inv3 * ld.intensity;
+                lt::TreeLightIn tl;
+                lt::Box tb; tb.mn = a; tb.mx = a;
+                lt::Box pb; pb.mn = b; pb.mx = b;
+                tb = lt::Box::unite(tb, pb);
+                pb.mn = cc; pb.mx = cc;
+                tb = lt::Box::unite(tb, pb);
+                tl.b = tb;
+                const float inv2a = (float)(areas[t] * 2.);
+                tl.dir = {cr.x / inv2a, cr.y / inv2a, cr.z / inv2a};
+                tl.dir = lt::V3f{cr.x * (1.f / inv2a), cr.y * (1.f / inv2a), cr.z * (1.f / inv2a)};
+                tl.power = irradiance * areas[t];
+                treeIn.push_back(tl);
+                treeRef.push_back(make_int2(i, (int)t));
+            }
+            L.num_tris = (int)m.num_triangles;
+            L.integral = lt::piecewise1d(areas.data(), m.num_triangles, fpool, L.dist_off);
+            L.power = ld.intensity * (meshArea * .5f);
+        } else if (ld.type == LGPU_LIGHT_POINT || ld.type == LGPU_LIGHT_SPOT) {
+            L.type = ld.type == LGPU_LIGHT_POINT ? LT_POINT : LT_SPOT;
+            L.pos = make_float3(ld.position[0], ld.position[1], ld.position[2]);
+            L.axis = make_float3(ld.axis[0], ld.axis[1], ld.axis[2]);
+            L.cosCone = std::cos(ld.cone_angle);
+            L.cosFall = std::cos(ld.falloff_start);
+            L.power = L.type == LT_POINT ? ld.intensity * (4 * PIf)
+                                         : ld.intensity * (2.f * PIf - (1 - .5f * (L.cosFall + L.cosCone)));
+        } else if (ld.type == LGPU_LIGHT_ENVIRONMENT) {
+            if (envLight >= 0) return fail(c, LGPU_ERR_INVALID_SCENE, "more than one environment light");
+            if (!ld.env_texture || ld.env_width <= 0 || ld.env_height <= 0) return fail(c, LGPU_ERR_INVALID_SCENE, "environment light without texture");
+            L.type = LT_ENV;
+            envLight = i;
+            const int w = ld.env_width, h = ld.env_height;
+            env.w = w; env.h = h; env.present = 1; env.intensity = ld.intensity;
+            env.offx = ld.offset[0]; env.offy = ld.offset[1];
+            env.tex_off = (int)envTex.size();
+            for (int k = 0; k < w * h; ++k) envTex.push_back(make_float4(ld.env_texture[3 * k], ld.env_texture[3 * k + 1], ld.env_texture[3 * k + 2], 0.f));
+            /* EnvironmentLight constructor (EnvironmentLight.cpp:9-22): luminance * sin(theta) */
+            std::vector<float> img((size_t)w * h);
+            for (int y = 0; y < h; ++y) {
+                const float vp = (float)y / (float)h;
+                const float sinT = std::sin(PIf * float(y + .5) / float(h));
+                for (int x = 0; x < w; ++x) {
+                    const float up = (float)x / (float)w;
+                    /* bilinear fetch at a texel corner = that texel */
+                    const float fx = std::min((float)(w - 1), std::max(std::min(up, 1.f), 0.f) * (float)w);
+                    const float fy = std::min((float)(h - 1), std::max(std::min(vp, 1.f), 0.f) * (float)h);
+                    const unsigned xi = (unsigned)fx, yi = (unsigned)fy;
+                    const unsigned x1 = std::min(xi + 1, (unsigned)w - 1), y1 = std::min(yi + 1, (unsigned)h - 1);
+                    const float *t00 = ld.env_texture + 3 * ((size_t)yi * w + xi), *t10 = ld.env_texture + 3 * ((size_t)yi * w + x1);
+                    const float *t01 = ld.env_texture + 3 * ((size_t)y1 * w + xi), *t11 = ld.env_texture + 3 * ((size_t)y1 * w + x1);
+                    float rgb[3];
+                    for (int k = 0; k < 3; ++k) {
+                        const float ya = t00[k] + (t10[k] - t00[k]) * (fx - (float)xi);
+                        const float yb = t01[k] + (t11[k] - t01[k]) * (fx - (float)xi);
+                        rgb[k] = ya + (yb - ya) * (fy - (float)yi);
+                    }
+                    const float lum = 0.212671f * rgb[0] + 0.715160f * rgb[1] + 0.072169f * rgb[2];
+                    img[x + (size_t)y * w] = std::abs(lum) * sinT;
+                }
+            }
+            /* Piecewise2D: per row CDF (w+1) + func (w) + integral (1); marginal CDF + func */
+            std::vector<float> rowInt(h);
+            env.cond_off = (int)fpool.size();
+            for (int y = 0; y < h; ++y) {
+                int off;
+                rowInt[y] = lt::piecewise1d(&img[(size_t)y * w], (unsigned)w, fpool, off);
+                fpool.push_back(rowInt[y]);
+            }
+            env.marg_integral = lt::piecewise1d(rowInt.data(), (unsigned)h, fpool, env.marg_off);
+            const float radius = std::max(std::max(sceneBox.mx.x - sceneBox.mn.x, sceneBox.mx.y - sceneBox.mn.y), sceneBox.mx.z - sceneBox.mn.z);
+            L.power = ld.intensity * (PIf * radius * radius);
+        } else {
+            return fail(c, LGPU_ERR_INVALID_SCENE, "unknown light type");
+        }
+        lightPower[i] = L.power;
+        if (L.type == LT_POINT || L.type == LT_SPOT) {
+            lt::TreeLightIn tl;
+            tl.b.mn = v3(ld.position); tl.b.mx = tl.b.mn;
+            tl.dir = L.type == LT_POINT ? lt::V3f{0, 1, 0} : v3(ld.axis);
+            tl.power = L.power;
+            treeIn.push_back(tl);
+            treeRef.push_back(make_int2(i, -1));
+        }
+    }
+    S.env = env;
+    S.env_light = envLight;
+    /* tree lights: triangle lights first (input order), then point / spot lights (ManyLightSampler::InitLights) */
+    {
+        std::vector<lt::TreeLightIn> ordered;
+        std::vector<int2> orderedRef;
+        for (size_t k = 0; k < treeIn.size(); ++k) if (treeRef[k].y >= 0) { ordered.push_back(treeIn[k]); orderedRef.push_back(treeRef[k]); }
+        for (size_t k = 0; k < treeIn.size(); ++k) if (treeRef[k].y < 0) { ordered.push_back(treeIn[k]); orderedRef.push_back(treeRef[k]); }
+        treeIn.swap(ordered);
+        treeRef.swap(orderedRef);
+        int base = 0;
+        for (int i = 0; i < d->num_lights; ++i)
+            if (lights[i].type == LT_MESH) { lights[i].tri_base = base; base += lights[i].num_tris; }
+    }
+    /* power sampler CDF (PowerLightSampler::Commit, LightSampler.cpp:25-35) */
+    {
+        float tot = 0;
+        for (int i = 0; i < d->num_lights; ++i) tot += lightPower[i];
+        S.power_integral = lt::piecewise1d(lightPower.data(), (unsigned)d->num_lights, fpool, S.power_cdf_off);
+        S.inv_total_power = 1.f / tot;
+    }
+    std::vector<int2> treeLights, treeSlot;
+    std::vector<DLNode> lnodes;
+    if (d->light_strategy == LGPU_LIGHT_STRATEGY_TREE) {
+        lt::TreeOut to;
+        lt::build_light_tree(treeIn, fpool, to);
+        lnodes = to.nodes;
+        S.tree_root = to.root;
+        S.tree_power = to.tree_power;
+        S.inf_power = envLight >= 0 ? lightPower[envLight] * .1f : 0.f;
+        S.num_tree_lights = (int)treeIn.size();
+        treeLights.resize(to.order.size());
+        for (size_t k = 0; k < to.order.size(); ++k) treeLights[k] = treeRef[to.order[k]];
+        /* input index -> (leaf, slot) */
+        std::vector<int2> slotOfInput(treeIn.size(), make_int2(-1, -1));
+        for (size_t ni = 0; ni < lnodes.size(); ++ni) {
+            const DLNode &n = lnodes[ni];
+            if (n.child0 >= 0) continue;
+            for (int k = 0; k < n.num; ++k) slotOfInput[to.order[n.first + k]] = make_int2((int)ni, k);
+        }
+        /* tree_slot is indexed by: mesh lights -> tri_base + tri, other lights -> their slot index */
+        treeSlot.resize(treeIn.size());
+        for (size_t k = 0; k < treeIn.size(); ++k) {
+            const int2 r = treeRef[k];
+            if (r.y >= 0) treeSlot[lights[r.x].tri_base + r.y] = slotOfInput[k];
+            else { lightSlot[r.x] = (int)k; treeSlot[k] = slotOfInput[k]; }
+        }
+        if (treeIn.empty() && envLight < 0) return fail(c, LGPU_ERR_INVALID_SCENE, "light tree is empty");
+    }
+
+    /* ---------------- media */
+    std::vector<DMedium> media(d->num_media);
+    for (int i = 0; i < d->num_media; ++i) {
+        DMedium &m = media[i];
+        std::memset(&m, 0, sizeof(m));
+        for (int k = 0; k < 3; ++k) { m.sa[k] = d->media[i].sigma_a[k]; m.ss[k] = d->media[i].sigma_s[k]; }
+        m.g = d->media[i].g;
+    }
+
+    /* ---------------- upload */
+    bool ok = upload(c, nodes, &S.nodes, bytes) && upload(c, tris, &S.tris, bytes) && upload(c, insts, &S.insts, bytes) &&
+              upload(c, objects, &S.objects, bytes) && upload(c, meshes, &S.meshes, bytes) && upload(c, pos, &S.pos, bytes) &&
+              upload(c, nrm, &S.nrm, bytes) && upload(c, tan, &S.tan, bytes) && upload(c, uv, &S.uv, bytes) &&
+              upload(c, tri_idx, &S.tri_idx, bytes) && upload(c, mats, &S.materials, bytes) && upload(c, code, &S.prog, bytes) &&
+              upload(c, lights, &S.lights, bytes) && upload(c, lnodes, &S.lnodes, bytes) &&
+              upload(c, treeLights, &S.tree_lights, bytes) && upload(c, treeSlot, &S.tree_slot, bytes) &&
+              upload(c, lightSlot, &S.light_slot, bytes) && upload(c, fpool, &S.fpool, bytes) &&
+              upload(c, envTex, &S.env_tex, bytes) && upload(c, media, &S.media, bytes);
+    if (!ok) { free_scene(c); return c->err.find("alloc") != std::string::npos ? LGPU_ERR_OOM : LGPU_ERR_CUDA; }
+    c->S = S;
+    c->have_scene = true;
+    c->stats.bvh_nodes = nodes.size();
+    c->stats.bvh_bytes = nodes.size() * sizeof(DNode);
+    c->stats.tri_bytes = tris.size() * sizeof(DTri);
+    c->stats.node_bytes = sizeof(DNode);
+    c->stats.tri_record_bytes = sizeof(DTri);
+    c->stats.device_bytes = bytes;
+    return LGPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+CamParams make_cam(const lgpu_camera_desc *cd, const lgpu_render_opts *o) {
+    CamParams cam;
+    cam.o = make_float3(cd->origin[0], cd->origin[1], cd->origin[2]);
+    cam.x = make_float3(cd->x_hat[0], cd->x_hat[1], cd->x_hat[2]);
+    cam.y = make_float3(cd->y_hat[0], cd->y_hat[1], cd->y_hat[2]);
+    cam.z = make_float3(cd->z_hat[0], cd->z_hat[1], cd->z_hat[2]);
+    cam.tanFov = (float)std::tan(.5 * cd->fov);   /* Camera::SetFov (Camera.cpp:34-37) */
+    cam.tanFov2 = 2 * cam.tanFov;
+    cam.aspect = (float)o->height / (float)o->width;
+    cam.xi = 1.f / (float)o->width;
+    cam.yi = 1.f / (float)o->height;
+    cam.W = o->width;
+    cam.H = o->height;
+    return cam;
+}
+
+int check_opts(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o) {
+    if (!c || !cam || !o) return LGPU_ERR_INVALID_ARG;
+    if (!c->have_scene) return fail(c, LGPU_ERR_NO_SCENE, "no committed scene");
+    if (o->width <= 0 || o->height <= 0 || o->spp <= 0) return fail(c, LGPU_ERR_INVALID_ARG, "width, height and spp must be positive");
+    if (o->max_bounces < 0 || o->min_bounces < 0) return fail(c, LGPU_ERR_INVALID_ARG, "negative bounce count");
+    if ((uint64_t)o->width * o->height > (1ull << 32) - 1) return fail(c, LGPU_ERR_INVALID_ARG, "film too large");
+    if (o->integrator != LGPU_INTEGRATOR_GPU_MISVOLPATH && o->integrator != LGPU_INTEGRATOR_VOLPATH)
+        return fail(c, LGPU_ERR_INVALID_ARG, "integrator not available on the GPU path");
+    return LGPU_OK;
+}
+
+int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o, float4 *film, float4 *paths,
+                const uint64_t *ids, uint64_t n, bool count, cudaStream_t s) {
+    LaunchArgs a;
+    a.S = c->S;
+    a.cam = make_cam(cam, o);
+    a.rp.spp = o->spp;
+    a.rp.max_bounces = o->max_bounces;
+    a.rp.min_bounces = o->min_bounces;
+    a.rp.seed = o->seed;
+    a.rp.sample_offset = o->sample_offset;
+    a.film = film;
+    a.paths_out = paths;
+    a.ids = ids;
+    a.n = n;
+    a.counters = c->d_counters;
+    a.hero = o->spectral_mode == LGPU_SPECTRAL_HERO4;
+    a.count = count;
+    a.stream = s;
+    if (count) cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
+    cudaEventRecord(c->ev0, s);
+    cudaError_t e = launch_render(a);
+    if (e != cudaSuccess) return cuda_fail(c, e, "render launch");
+    cudaEventRecord(c->ev1, s);
+    c->stats.paths = n;
+    return LGPU_OK;
+}
+
+int finish_timing(lgpu_context *c) {
+    cudaError_t e = cudaEventSynchronize(c->ev1);
+    if (e != cudaSuccess) return cuda_fail(c, e, "render");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->stats.last_render_ms = ms;
+    return LGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+LGPU_API int lgpu_render_device(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o,
+                                float *film_dev, float *path_out_dev, void *stream) {
+    int r = check_opts(c, cam, o);
+    if (r) return r;
+    cudaSetDevice(c->device);
+    const uint64_t n = (uint64_t)o->width * o->height * o->spp;
+    return render_impl(c, cam, o, reinterpret_cast<float4 *>(film_dev), reinterpret_cast<float4 *>(path_out_dev), nullptr, n,
+                       false, (cudaStream_t)stream);
+}
+
+LGPU_API int lgpu_render(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o, float *film_rgbn) {
+    int r = check_opts(c, cam, o);
+    if (r) return r;
+    if (!film_rgbn) return fail(c, LGPU_ERR_INVALID_ARG, "null film");
+    cudaSetDevice(c->device);
+    const size_t px = (size_t)o->width * o->height;
+    if (c->film_px < px) {
+        cudaFree(c->d_film);
+        c->d_film = nullptr;
+        cudaError_t e = cudaMalloc(&c->d_film, px * sizeof(float4));
+        if (e != cudaSuccess) { c->film_px = 0; return cuda_fail(c, e, "film allocation"); }
+        c->film_px = px;
+    }
+    cudaError_t e = cudaMemcpy(c->d_film, film_rgbn, px * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(c, e, "film upload");
+    const uint64_t n = (uint64_t)px * o->spp;
+    r = render_impl(c, cam, o, c->d_film, nullptr, nullptr, n, false, 0);
+    if (r) return r;
+    r = finish_timing(c);
+    if (r) return r;
+    e = cudaMemcpy(film_rgbn, c->d_film, px * sizeof(float4), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "film download");
+    return LGPU_OK;
+}
+
+LGPU_API int lgpu_render_paths(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o,
+                               const uint64_t *path_ids, uint64_t n, float *path_out_host) {
+    int r = check_opts(c, cam, o);
+    if (r) return r;
+    if (!path_ids || !path_out_host) return fail(c, LGPU_ERR_INVALID_ARG, "null path buffers");
+    cudaSetDevice(c->device);
+    const uint64_t total = (uint64_t)o->width * o->height * o->spp;
+    for (uint64_t i = 0; i < n; ++i)
+        if (path_ids[i] >= total) return fail(c, LGPU_ERR_INVALID_ARG, "path id out of range");
+    if (c->ids_cap < n) {
+        cudaFree(c->d_ids);
+        c->d_ids = nullptr;
+        cudaError_t e = cudaMalloc(&c->d_ids, n * sizeof(uint64_t));
+        if (e != cudaSuccess) { c->ids_cap = 0; return cuda_fail(c, e, "id buffer"); }
+        c->ids_cap = n;
+    }
+    if (c->paths_cap < n) {
+        cudaFree(c->d_paths);
+        c->d_paths = nullptr;
+        cudaError_t e = cudaMalloc(&c->d_paths, n * sizeof(float4));
+        if (e != cudaSuccess) { c->paths_cap = 0; return cuda_fail(c, e, "path buffer"); }
+        c->paths_cap = n;
+    }
+    cudaError_t e = cudaMemcpy(c->d_ids, path_ids, n * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(c, e, "id upload");
+    r = render_impl(c, cam, o, nullptr, c->d_paths, c->d_ids, n, false, 0);
+    if (r) return r;
+    r = finish_timing(c);
+    if (r) return r;
+    e = cudaMemcpy(path_out_host, c->d_paths, n * sizeof(float4), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "path download");
+    return LGPU_OK;
+}
+
+LGPU_API int lgpu_render_count(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o) {
+    int r = check_opts(c, cam, o);
+    if (r) return r;
+    cudaSetDevice(c->device);
+    const uint64_t n = (uint64_t)o->width * o->height * o->spp;
+    r = render_impl(c, cam, o, nullptr, nullptr, nullptr, n, true, 0);
+    if (r) return r;
+    r = finish_timing(c);
+    if (r) return r;
+    unsigned long long h[4];
+    cudaError_t e = cudaMemcpy(h, c->d_counters, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "counter download");
+    c->stats.nodes_visited = h[0];
+    c->stats.tris_tested = h[1];
+    c->stats.rays = h[2];
+    return LGPU_OK;
+}
+
+LGPU_API int lgpu_intersect(lgpu_context *c, const float *rays_dev, uint32_t *hits_dev, float *uv_out_dev, uint64_t n, void *stream) {
+    if (!c || !rays_dev || !hits_dev) return LGPU_ERR_INVALID_ARG;
+    if (!c->have_scene) return fail(c, LGPU_ERR_NO_SCENE, "no committed scene");
+    cudaSetDevice(c->device);
+    cudaError_t e = launch_intersect(c->S, rays_dev, hits_dev, uv_out_dev, n, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "intersect launch");
+    e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "intersect");
+    return LGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,40 @@
+/*
+ * Host-side scene compilation for the GB300 path tracer: BVH2 construction (binned SAH), the
+ * light-tree build of ManyLightSampler and the shader-graph compiler.  Internal to the module.
+ */
+#pragma once
+#include <string>
+#include <vector>
+#include "lgpu_scene.h"
+#include "../../include/lambda_gpu.h"
+
+namespace lg {
+
+struct Aabb {
+    float lo[3], hi[3];
+};
+
+/* Binned-SAH BVH2 over primitive boxes.  Output nodes are numbered from 0 (the root); child refs are
+ * encoded (index << 4) | count with count 0 for inner nodes.  `order` receives the primitive order of
+ * the leaves; leaf first indices point into that order plus `prim_base`. */
+struct BvhOut {
+    std::vector<DNode> nodes;
+    std::vector<uint32_t> order;
+    int root_ref = 0;
+    int max_depth = 0;
+};
+void build_bvh(const std::vector<Aabb> &boxes, int max_leaf, int node_base, int prim_base, BvhOut &out);
+
+/* Shader-graph compiler: DAG -> linear bytecode with one register per live value. */
+struct GraphCompiler {
+    const lgpu_scene_desc *d = nullptr;
+    std::vector<DIns> *code = nullptr;
+    std::string err;
+    /* compile the BSDF of a material into m (program appended to *code) */
+    bool compile_material(int bxdf_node, DMaterial &m);
+    /* compile a light's emission socket; out_reg receives the illuminant spectrum register,
+     * out_reg + 1 the reflectance one */
+    bool compile_emission(int node, int socket, int &prog_off, int &prog_len, int &out_reg);
+};
+
+}  // namespace lg

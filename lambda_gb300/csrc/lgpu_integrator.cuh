@@ -1,0 +1,605 @@
+/*
+ * Lights, light sampling, transmittance queries and the MIS volumetric integrator on the GPU.
+ * Restates src/lighting/ (Light.cpp, MeshLight.cpp, PointLight.cpp, Spotlight.cpp,
+ * EnvironmentLight.cpp, LightSampler.cpp, ManyLightSampler.cpp), src/core/Scene.cpp:28-107 and
+ * src/integrators/MISVolumetricPathIntegrator.cpp:23-215 for one path per thread.
+ */
+#pragma once
+#include "lgpu_device.cuh"
+
+namespace lg {
+
+/* A light as the integrator sees it: `tri` >= 0 selects a TriangleLight of mesh light `light`
+ * (the light tree's unit), tri = -1 the light itself.  Equality is pointer equality in the
+ * reference (`nl != l`). */
+struct LRef { int light, tri; };
+
+#define LG_MAX_TREE_DEPTH 48
+HD bool lref_eq(LRef a, LRef b) { return a.light == b.light && a.tri == b.tri; }
+
+template <int NS, bool COUNT>
+struct Tracer {
+    const DeviceScene &S;
+    Rng &rng;
+    const Lambda4 &lam;
+    TravStats *st;
+
+    /* ---------------------------------------------------------------- scene queries */
+    __device__ bool intersect(float3 o, float3 d, RayHit &h) {   /* Scene::Intersect (Scene.cpp:28-43) */
+        HitRec hr;
+        if (!traverse<COUNT>(S, o, d, finf(), false, &hr, st)) return false;
+        if (!(hr.t > 0.f) || !(hr.t < finf())) return false;
+        process_hit(S, o, d, hr, h);
+        return true;
+    }
+    __device__ bool occluded(float3 o, float3 d, float tmax) {
+        HitRec hr;
+        return traverse<COUNT>(S, o, d, tmax, true, &hr, st);
+    }
+    __device__ const DMaterial &mat(const RayHit &h) { return S.materials[S.objects[h.obj].material]; }
+    __device__ int get_medium(const DMaterial &m, float3 w, float3 n) { return dot(w, n) < 0.f ? m.medium_interior : m.medium_exterior; }
+
+    /* Scene::IntersectTr (Scene.cpp:45-81); maxT < 0 selects the unbounded form. */
+    __device__ bool intersect_tr(float3 o, float3 d, RayHit &h, int med, Spec<NS> *Tr, float maxT) {
+        float tFar = 0.f;
+        for (int guard = 0; guard < 256; ++guard) {
+            if (!intersect(o, d, h)) return false;
+            tFar += h.tFar;
+            bool term = false;
+            if (maxT >= 0.f) {
+                term = tFar > maxT;
+                if (term) { const float delta = tFar - maxT; tFar -= delta; h.tFar -= delta; }
+            }
+            if (med >= 0 && Tr) *Tr *= medium_tr<NS>(S.media[med], h.tFar);
+            const DMaterial &m = mat(h);
+            if (term || m.has_bsdf || m.light >= 0) { h.tFar = tFar; return true; }
+            med = get_medium(m, d, h.nG);
+            o = h.point + h.nG * (dot(h.nG, d) < 0.f ? -SURFACE_EPSILON : SURFACE_EPSILON);
+        }
+        return false;
+    }
+    /* Light::MutualVisibility / PointMutualVisibility (Light.cpp:10-38); bounded = point form. */
+    __device__ bool light_visibility(float3 p1, float3 p2, Event &ev, Spec<NS> *Tr, bool bounded) {
+        const float3 diff = p2 - p1;
+        const float m = mag(diff);
+        const float3 dir = divs(diff, m);
+        if (S.has_volumes) {
+            const float minT = m - SURFACE_EPSILON * 10.f;
+            ev.wi = dir;
+            RayHit hh;
+            hh.tFar = finf();
+            intersect_tr(p1, dir, hh, ev.medium, Tr, bounded ? m : -1.f);
+            return hh.tFar > minT;
+        }
+        ev.wi = dir;   /* Scene::MutualVisibility (Scene.cpp:83-95) */
+        return !occluded(p1, dir, (float)(m - .00001));
+    }
+    /* Light::RayEscapes (Light.cpp:40-49) */
+    __device__ bool ray_escapes(float3 o, float3 d, const Event &ev, Spec<NS> *Tr) {
+        if (S.has_volumes) {
+            RayHit hh;
+            return !intersect_tr(o, d, hh, ev.medium, Tr, -1.f);
+        }
+        return !occluded(o, d, finf());
+    }
+
+    /* ---------------------------------------------------------------- emission programs */
+    __device__ Spec<NS> emission(const DLight &L, const Event &ev, const RayHit &h, bool illum) {
+        float4 R[LGPU_MAX_REGS];
+        ShadeCtx c;
+        c.point = h.point; c.normalS = h.nS; c.uv = h.uv; c.woLy = ev.woL.y; c.eta = ev.eta;
+        c.mediumInteraction = ev.mediumInteraction;
+        run_prog<NS>(S.prog + L.prog_off, L.prog_len, c, lam, R);
+        /* the program ends with a conversion to a spectrum; the reflectance variant sits one
+         * register above the illuminant one */
+        return Spec<NS>::from4(R[L.out_reg + (illum ? 0 : 1)]);
+    }
+
+    /* ---------------------------------------------------------------- environment light */
+    __device__ Spec<NS> env_texel_uv(float u, float v) {   /* TextureAdapter::GetUV, bilinear (Texture.h:71-81) */
+        const DEnv &E = S.env;
+        u = fractf(u); v = fractf(v);
+        const float fx = fminf((float)(E.w - 1), clampr(u, 0.f, 1.f) * (float)E.w);
+        const float fy = fminf((float)(E.h - 1), clampr(v, 0.f, 1.f) * (float)E.h);
+        const unsigned x = (unsigned)fx, y = (unsigned)fy;
+        const unsigned x1 = min(x + 1, (unsigned)E.w - 1), y1 = min(y + 1, (unsigned)E.h - 1);
+        const float4 a = __ldg(&S.env_tex[E.tex_off + y * E.w + x]), b = __ldg(&S.env_tex[E.tex_off + y * E.w + x1]);
+        const float4 c = __ldg(&S.env_tex[E.tex_off + y1 * E.w + x]), d = __ldg(&S.env_tex[E.tex_off + y1 * E.w + x1]);
+        const float tx = fx - (float)x, ty = fy - (float)y;
+        const float r = lerpf(lerpf(a.x, b.x, tx), lerpf(c.x, d.x, tx), ty);
+        const float g = lerpf(lerpf(a.y, b.y, tx), lerpf(c.y, d.y, tx), ty);
+        const float bb = lerpf(lerpf(a.z, b.z, tx), lerpf(c.z, d.z, tx), ty);
+        return from_rgb<NS>(r, g, bb, true, lam);
+    }
+    __device__ Spec<NS> env_le(float3 w) {   /* EnvironmentLight::Le (EnvironmentLight.h:47-50) */
+        const DEnv &E = S.env;
+        const float u = fractf((spherical_phi(w) - E.offx) * INV_PI2);
+        const float v = fractf((spherical_theta(w) - E.offy) * INV_PI);
+        return env_texel_uv(u, v) * E.intensity;
+    }
+    __device__ float p1d_sample_cont(int cdf_off, int n, float integral, float u, float *pdf, int *off_) {
+        const float *cdf = S.fpool + cdf_off;
+        const int off = find_interval(cdf, n + 1, u);
+        if (off_) *off_ = off;
+        float du = u - cdf[off];
+        if ((cdf[off + 1] - cdf[off]) > 0.f) du /= (cdf[off + 1] - cdf[off]);
+        *pdf = S.fpool[cdf_off + n + 1 + off] / integral;
+        return ((float)off + du) / (float)n;
+    }
+    __device__ Spec<NS> env_sample_li(Event &ev, const RayHit &h, float &pdf) {   /* EnvironmentLight.cpp:24-45 */
+        const DEnv &E = S.env;
+        const float u0 = rng.next(), u1 = rng.next();
+        float pm, pc; int row;
+        const float d1 = p1d_sample_cont(E.marg_off, E.h, E.marg_integral, u1, &pm, &row);
+        const int co = E.cond_off + row * (2 * E.w + 2);
+        const float d0 = p1d_sample_cont(co, E.w, S.fpool[co + 2 * E.w + 1], u0, &pc, nullptr);
+        pdf = pc * pm;
+        if (pdf == 0.f) return Spec<NS>(0.f);
+        const float theta = d1 * PI + E.offy;
+        const float phi = d0 * PI2 + E.offx;
+        const float cT = cosf(theta), sT = sinf(theta);
+        if (sT == 0.f) { pdf = 0.f; return Spec<NS>(0.f); }
+        ev.wi = spherical_dir(sT, cT, phi);
+        Spec<NS> Tr(1.f);
+        if (ray_escapes(h.point + h.nG * SURFACE_EPSILON, ev.wi, ev, &Tr)) {
+            ev.wiL = ev_local(h, ev.wi);
+            pdf /= 2.f * PI * PI * sT;
+            return env_texel_uv(d0, d1) * Tr * E.intensity;
+        }
+        pdf = 0.f;
+        return Spec<NS>(0.f);
+    }
+    __device__ float env_pdf_li(const Event &ev) {   /* EnvironmentLight.cpp:60-67 + Piecewise2D::PDF */
+        const DEnv &E = S.env;
+        const float theta = spherical_theta(ev.wi) - E.offy;
+        const float phi = spherical_phi(ev.wi) - E.offx;
+        const float sT = sinf(theta);
+        if (sT == 0.f) return 0.f;
+        const float u = fractf(phi * INV_PI2), v = fractf(theta * INV_PI);
+        const int iu = max(min((int)(u * (float)E.w), E.w - 1), 0);
+        const int iv = max(min((int)(v * (float)E.h), E.h - 1), 0);
+        const int co = E.cond_off + iv * (2 * E.w + 2);
+        const float p = S.fpool[co + E.w + 1 + iu] / E.marg_integral;
+        return p / (2.f * PI * PI * sT);
+    }
+
+    /* ---------------------------------------------------------------- mesh / triangle lights */
+    __device__ void tri_verts(const DLight &L, int t, float3 &a, float3 &b, float3 &c) {
+        const DObject &ob = S.objects[L.object];
+        const DMesh me = S.meshes[ob.mesh];
+        const uint4 ti = __ldg(&S.tri_idx[me.tri_off + t]);
+        a = f3(__ldg(&S.pos[me.vtx_off + ti.x]));
+        b = f3(__ldg(&S.pos[me.vtx_off + ti.y]));
+        c = f3(__ldg(&S.pos[me.vtx_off + ti.z]));
+    }
+    __device__ float2 tri_uv(const DLight &L, int t, float u, float v) {
+        const DObject &ob = S.objects[L.object];
+        const DMesh me = S.meshes[ob.mesh];
+        const uint4 ti = __ldg(&S.tri_idx[me.tri_off + t]);
+        const float2 a = S.uv[me.vtx_off + ti.x], b = S.uv[me.vtx_off + ti.y], c = S.uv[me.vtx_off + ti.z];
+        return make_float2(a.x + (b.x - a.x) * u + (c.x - a.x) * v, a.y + (b.y - a.y) * u + (c.y - a.y) * v);
+    }
+    __device__ bool mesh_has_uv(const DLight &L) { return (S.meshes[S.objects[L.object].mesh].flags & 2) != 0; }
+    HD static void area_normal(float3 a, float3 b, float3 c, float *area, float3 *n) {   /* TriangleMesh.h:59-63 */
+        const float3 cr = cross(b - a, c - a);
+        *area = mag(cr) * .5f;
+        if (n) *n = divs(cr, (float)(*area * 2.));
+    }
+    __device__ int mesh_pick(const DLight &L, float u, float *pdf) {   /* Piecewise1D::SampleDiscrete */
+        const float *cdf = S.fpool + L.dist_off;
+        const int off = find_interval(cdf, L.num_tris + 1, u);
+        *pdf = S.fpool[L.dist_off + L.num_tris + 1 + off] / (L.integral * (float)L.num_tris);
+        return off;
+    }
+
+    /* Light::Sample_Li for every light kind. */
+    __device__ Spec<NS> sample_li(LRef r, Event &ev, RayHit &h, float &pdf) {
+        if (r.light < 0) { pdf = 0.f; return Spec<NS>(0.f); }   /* no light to sample */
+        const DLight &L = S.lights[r.light];
+        if (L.type == LT_ENV) return env_sample_li(ev, h, pdf);
+        if (L.type == LT_POINT || L.type == LT_SPOT) {   /* PointLight.cpp:18-29, Spotlight.cpp:44-55 */
+            const float3 p = h.point + h.nG * SURFACE_EPSILON * (float)ev.sidedness;
+            Spec<NS> Tr(1.f);
+            if (light_visibility(p, L.pos, ev, &Tr, true)) {
+                pdf = 1.f;
+                const float d2 = distsq(L.pos, h.point);
+                ev.wiL = ev_local(h, ev.wi);
+                Spec<NS> e = emission(L, ev, h, false) * Tr;
+                if (L.type == LT_SPOT) e = e * spot_falloff(L, -ev.wi);
+                return e * L.intensity / d2;
+            }
+            pdf = 0.f;
+            return Spec<NS>(0.f);
+        }
+        /* mesh light: whole mesh (MeshLight.cpp:22-42) or one triangle (TriangleLight, :134-151) */
+        int t = r.tri;
+        float u0, u1;
+        if (t < 0) {
+            t = mesh_pick(L, rng.next(), &pdf);
+            u0 = rng.next(); u1 = rng.next();
+        } else {
+            u0 = rng.next(); u1 = rng.next();
+        }
+        float3 a, b, c;
+        tri_verts(L, t, a, b, c);
+        const float3 pL = a + (b - a) * u0 + (c - a) * u1;
+        const float3 pS = h.point + h.nG * SURFACE_EPSILON * (float)ev.sidedness;
+        Spec<NS> Tr(1.f);
+        if (light_visibility(pS, pL, ev, &Tr, false)) {
+            float area; float3 n;
+            area_normal(a, b, c, &area, &n);
+            const float cT = fabsf(dot(n, -ev.wi));
+            if (cT > 0.f) {
+                ev.wiL = ev_local(h, ev.wi);
+                if (r.tri < 0) pdf *= distsq(h.point, pL) / (cT * area);
+                else pdf = distsq(h.point, pL) / (cT * area);   /* B10 */
+                return emission(L, ev, h, true) * Tr * L.intensity * INV_PI;
+            }
+        }
+        pdf = 0.f;
+        return Spec<NS>(0.f);
+    }
+    __device__ float spot_falloff(const DLight &L, float3 w) {   /* Spotlight.cpp:21-27 */
+        const float c = dot(w, L.axis);
+        if (c < L.cosCone) return 0.f;
+        if (c > L.cosFall) return 1.f;
+        const float d = (c - L.cosCone) / (L.cosFall - L.cosCone);
+        return (d * d) * (d * d);
+    }
+    /* Light::PDF_Li(event) at the new hit (MeshLight.cpp:44-53, :158-165, EnvironmentLight.cpp:60-67). */
+    __device__ float pdf_li(LRef r, const Event &ev, const RayHit &h) {
+        const DLight &L = S.lights[r.light];
+        if (L.type == LT_ENV) return env_pdf_li(ev);
+        if (L.type != LT_MESH) return 0.f;
+        if (dot(ev.wi, h.nG) > 0.f) return 0.f;
+        const float distSq = h.tFar * h.tFar;
+        float3 a, b, c;
+        tri_verts(L, h.prim, a, b, c);
+        float area;
+        area_normal(a, b, c, &area, nullptr);
+        const float cT = fabsf(dot(h.nG, -ev.wi));
+        if (r.tri < 0) {
+            const float triPdf = S.fpool[L.dist_off + L.num_tris + 1 + h.prim];   /* raw area (Piecewise1D::PDF) */
+            return triPdf * distSq / (cT * area);
+        }
+        return distSq / (cT * area);
+    }
+    /* Light::SamplePoint (MeshLight.cpp:55-70, :167-181, PointLight.cpp:40-44). */
+    __device__ Spec<NS> sample_point(LRef r, Event &ev, RayHit &h, float3 &lpoint, float3 &lnormal, float &lpdf) {
+        if (r.light < 0) { lpdf = 0.f; lpoint = h.point; return Spec<NS>(0.f); }
+        const DLight &L = S.lights[r.light];
+        if (L.type == LT_ENV) { lpdf *= 0.f; lpoint = mk(0.f, 0.f, 0.f); return Spec<NS>(0.f); }
+        if (L.type == LT_POINT || L.type == LT_SPOT) { lpoint = L.pos; return emission(L, ev, h, true) * L.intensity; }
+        int t = r.tri;
+        float3 a, b, c;
+        if (t < 0) {
+            float dp;
+            t = mesh_pick(L, rng.next(), &dp);
+            tri_verts(L, t, a, b, c);
+            float area;
+            area_normal(a, b, c, &area, &lnormal);
+            lpdf *= dp / area;
+        } else {
+            tri_verts(L, t, a, b, c);
+            float area;
+            area_normal(a, b, c, &area, nullptr);
+            lpdf /= area;
+        }
+        const float u0 = rng.next(), u1 = rng.next();
+        if (mesh_has_uv(L)) h.uv = tri_uv(L, t, u0, u1);
+        lpoint = a + (b - a) * u0 + (c - a) * u1;
+        return emission(L, ev, h, true) * L.intensity * INV_PI;
+    }
+    /* Light::Visibility (MeshLight.cpp:72-81, :183-192, PointLight.cpp:46-55, Spotlight.cpp:69-78, EnvironmentLight.cpp:76-84). */
+    __device__ Spec<NS> visibility(LRef r, float3 p, Event &ev, RayHit &h, float3 lpoint, float3 lnormal, float &lpdf) {
+        if (r.light < 0) { lpdf = 0.f; return Spec<NS>(0.f); }
+        const DLight &L = S.lights[r.light];
+        Spec<NS> Tr(1.f);
+        if (L.type == LT_ENV) {
+            const float3 wi = normalised(lpoint - p);
+            if (ray_escapes(p, wi, ev, &Tr)) return Tr;
+            lpdf = 0.f;
+            return Spec<NS>(0.f);
+        }
+        if (L.type == LT_POINT || L.type == LT_SPOT) {
+            const float3 q = p + h.nG * SURFACE_EPSILON * (float)ev.sidedness;
+            if (light_visibility(q, lpoint, ev, &Tr, true)) {
+                Spec<NS> v = Tr;
+                if (L.type == LT_SPOT) v = v * spot_falloff(L, -ev.wi);
+                return v / distsq(L.pos, h.point);
+            }
+            lpdf = 0.f;
+            return Spec<NS>(0.f);
+        }
+        if (light_visibility(p, lpoint, ev, &Tr, false)) {
+            const float cT = r.tri < 0 ? fabsf(dot(lnormal, -ev.wi)) : fabsf(dot(h.nG, -ev.wi));
+            lpdf *= distsq(p, lpoint) / cT;
+            return Tr;
+        }
+        lpdf = 0.f;
+        return Spec<NS>(0.f);
+    }
+    /* Light::L at the new hit (MeshLight::L) */
+    __device__ Spec<NS> light_L(LRef r, const Event &ev, const RayHit &h) {
+        const DLight &L = S.lights[r.light];
+        if (L.type == LT_ENV) return env_le(ev.wi);
+        if (L.type == LT_MESH) return emission(L, ev, h, true) * L.intensity * INV_PI;
+        return Spec<NS>(0.f);
+    }
+    __device__ Spec<NS> light_Le(LRef r, float3 d) {
+        const DLight &L = S.lights[r.light];
+        if (L.type == LT_ENV) return env_le(d);
+        return Spec<NS>(0.f);
+    }
+
+    /* ---------------------------------------------------------------- light samplers */
+    /* ManyLightSampler::ImportanceMeasure (ManyLightSampler.cpp:305-326) */
+    __device__ float importance(float3 p, float3 nS, const DLNode &n) {
+        const float3 cen = n.bmin + (n.bmax - n.bmin) * .5f;
+        float3 delta = cen - p;
+        const float diam = mag(n.bmax - n.bmin);
+        const float d2 = dot(delta, delta);
+        const float dd = sqrtf(d2);
+        const float invD = 1.f / dd;
+        delta = delta * invD;
+        const float theta = acosf(dot(delta, n.axis));
+        const float thetaU = atanf((diam * .5f) * invD);
+        const float thetaD = smax(theta - n.thetaO - thetaU, 0.f);
+        if (thetaD < n.thetaE) {
+            const float thetaI = acosf(dot(delta, nS));
+            return (cosf(smax(thetaI - thetaU, 0.f)) * n.power) / d2 * cosf(thetaD);
+        }
+        return 0.f;
+    }
+    __device__ LRef tree_light_ref(int idx) {
+        const int2 tl = __ldg(&S.tree_lights[idx]);
+        LRef r; r.light = tl.x; r.tri = tl.y;
+        return r;
+    }
+    /* LightSampler::Sample: PowerLightSampler (LightSampler.cpp:17-19) or ManyLightSampler (:17-27, :355-378). */
+    __device__ LRef sample_light(float3 p, float3 nS, float *pdf) {
+        if (S.light_strategy == LGPU_LIGHT_STRATEGY_POWER) {
+            const float *cdf = S.fpool + S.power_cdf_off;
+            const float u = rng.next();
+            const int off = find_interval(cdf, S.num_lights + 1, u);
+            *pdf = S.fpool[S.power_cdf_off + S.num_lights + 1 + off] / (S.power_integral * (float)S.num_lights);
+            LRef r; r.light = off; r.tri = -1;
+            return r;
+        }
+        float eps = rng.next();
+        const float pTree = S.tree_power / (S.inf_power + S.tree_power);
+        if (eps < pTree) {
+            eps /= pTree;
+            *pdf *= pTree;
+            float e = rng.next();   /* B6: a fresh draw drives the descent */
+            int ni = S.tree_root;
+            for (int guard = 0; guard < 64; ++guard) {
+                const DLNode &n = S.lnodes[ni];
+                if (n.child0 < 0) {
+                    const float *cdf = S.fpool + n.dist_off;
+                    const int off = find_interval(cdf, n.num + 1, e);
+                    *pdf *= S.fpool[n.dist_off + n.num + 1 + off] / (n.integral * (float)n.num);
+                    return tree_light_ref(n.first + off);
+                }
+                const float IL = importance(p, nS, S.lnodes[n.child0]);
+                const float IR = importance(p, nS, S.lnodes[n.child1]);
+                const float PL = IL / (IL + IR);
+                const float PR = 1.f - PL;
+                if (e < PL) { e /= PL; *pdf *= PL; ni = n.child0; }
+                else { e = (e - PL) / PR; *pdf *= PR; ni = n.child1; }
+            }
+        }
+        *pdf *= 1.f - pTree;
+        LRef r; r.light = S.env_light; r.tri = -1;
+        return r;
+    }
+    /* LightSampler::Pdf (LightSampler.cpp:21-23, ManyLightSampler.cpp:29-35 + RecursivePDF :380-393, B7, B8). */
+    __device__ float light_pdf(float3 p, float3 nS, int prim, LRef l) {
+        const DLight &L = S.lights[l.light];
+        if (S.light_strategy == LGPU_LIGHT_STRATEGY_POWER) return L.power * S.inv_total_power;
+        if (L.type == LT_ENV) return S.inf_power / (S.inf_power + S.tree_power);
+        int ti;
+        if (L.type == LT_MESH) ti = L.tri_base + (l.tri >= 0 ? l.tri : prim);
+        else ti = S.light_slot[l.light];
+        const int2 slot = __ldg(&S.tree_slot[ti]);
+        const DLNode &leaf = S.lnodes[slot.x];
+        const float pdf = S.fpool[leaf.dist_off + leaf.num + 1 + slot.y];   /* raw power (Piecewise1D::PDF) */
+        /* the reference multiplies the branch probabilities from the root down (recursion) */
+        float lev[LG_MAX_TREE_DEPTH];
+        int depth = 0;
+        int child = slot.x;
+        int ni = leaf.parent;
+        while (ni >= 0 && depth < LG_MAX_TREE_DEPTH) {
+            const DLNode &n = S.lnodes[ni];
+            const float IL = importance(p, nS, S.lnodes[n.child0]);
+            const float IR = importance(p, nS, S.lnodes[n.child1]);
+            const float p0 = IL / (IL + IR);
+            lev[depth++] = (child == n.child0) ? p0 : 1.f - p0;
+            child = ni;
+            ni = n.parent;
+        }
+        float acc = 1.f;
+        if (depth > 0) {
+            acc = lev[depth - 1];
+            for (int k = depth - 2; k >= 0; --k) acc = lev[k] * acc;
+        }
+        return pdf * acc;
+    }
+
+    /* ---------------------------------------------------------------- BSDF setup */
+    __device__ void setup_bsdf(Bsdf<NS> &b, const DMaterial &m, const Event &ev, const RayHit &h) {
+        b.m = &m;
+        float4 R[LGPU_MAX_REGS];
+        ShadeCtx c;
+        c.point = h.point; c.normalS = h.nS; c.uv = h.uv; c.woLy = ev.woL.y; c.eta = ev.eta;
+        c.mediumInteraction = ev.mediumInteraction;
+        run_prog<NS>(S.prog + m.prog_off, m.prog_len, c, lam, R);
+        for (int i = 0; i < m.num_leaves; ++i) {
+            b.alb[i] = Spec<NS>::from4(R[m.leaves[i].albedo]);
+            b.rough[i] = R[m.leaves[i].rough].x;
+        }
+        for (int i = 0; i < m.num_tree; ++i) b.ratio[i] = m.tree[i].kind ? R[m.tree[i].ratio].x : 0.f;
+    }
+
+    /* ---------------------------------------------------------------- integrator */
+    HD static float power_heuristic(float f, float g) { return (f * f) / (f * f + g * g); }
+
+    /* LdMediumPoint (MISVolumetricPathIntegrator.cpp:23-69) */
+    __device__ Spec<NS> ld_medium_point(Event &ev, RayHit &hit, float3 p, LRef lsLight, float3 lsPoint, float3 lsNormal,
+                                        Spec<NS> lsLe, float &lsPdf, float3 &wiOut, float3 sp, float3 sn) {
+        /* lsPdf is the PartialLightSample's pdf: Visibility completes it in place, so the second
+         * call (equiangular point) starts from the value the first call left. */
+        const DMedium &med = S.media[ev.medium];
+        float partialLightPDF = lsPdf;
+        hit.point = p;
+        Spec<NS> Li = lsLe * visibility(lsLight, p, ev, hit, lsPoint, lsNormal, lsPdf);
+        float scatteringPDF, lightPDF = lsPdf;
+        Spec<NS> Ld(0.f);
+        if (lightPDF > 0.f && !Li.black()) {
+            scatteringPDF = phase_hg(dot(ev.wo, ev.wi), med.g);
+            if (scatteringPDF > 0.f) {
+                const float w = power_heuristic(lightPDF, scatteringPDF);
+                Ld += Li * Spec<NS>(scatteringPDF) * w / lightPDF;
+            }
+        }
+        scatteringPDF = hg_sample(med.g, ev.wo, &ev.wi, rng);
+        wiOut = ev.wi;
+        const float3 ro = p, rd = ev.wi;
+        Spec<NS> Tr(1.f);
+        const bool hs = intersect_tr(ro, rd, hit, ev.medium, &Tr, -1.f);
+        if (scatteringPDF > 0.f) {
+            LRef nl; nl.light = hs ? mat(hit).light : S.env_light; nl.tri = -1;
+            if (nl.light >= 0) {
+                if (!lref_eq(nl, lsLight)) partialLightPDF = light_pdf(sp, sn, hit.prim, nl);
+                lightPDF = partialLightPDF * pdf_li(nl, ev, hit);
+                Li = hs ? light_L(nl, ev, hit) : light_Le(nl, rd);
+                const float w = power_heuristic(scatteringPDF, lightPDF);
+                if (!Li.black() && lightPDF > 0.f) Ld += Li * Tr * w / scatteringPDF;
+            }
+        }
+        return Ld;
+    }
+
+    /* MISVolumetricPathIntegrator::Li (MISVolumetricPathIntegrator.cpp:71-215) */
+    __device__ Spec<NS> Li(float3 ro, float3 rd, int maxBounces, int minBounces) {
+        Spec<NS> L(0.f), beta(1.f);
+        RayHit hit;
+        hit.tFar = finf(); hit.uv = make_float2(0.f, 0.f);
+        Event ev;
+        ev.wo = -rd; ev.wi = mk(0.f, 0.f, 0.f); ev.woL = ev.wi; ev.wiL = ev.wi;
+        ev.sidedness = 1; ev.medium = -1; ev.eta = 1.001f; ev.mediumInteraction = false;
+        bool scatterIntersect = false;
+        int nullCrossings = 0;   /* null surfaces do not count as bounces; bound them (256) */
+        for (int bounces = 0; bounces < maxBounces; ++bounces) {
+            if (bounces == 0 ? intersect(ro, rd, hit) : scatterIntersect) {
+                if (bounces == 0) {
+                    const int li = mat(hit).light;
+                    if (li >= 0) {
+                        LRef lr; lr.light = li; lr.tri = -1;
+                        if (ev.medium >= 0) L += light_L(lr, ev, hit) * medium_tr<NS>(S.media[ev.medium], hit.tFar);
+                        else L += light_L(lr, ev, hit);
+                    }
+                }
+                if (ev.medium >= 0) {
+                    const DMedium &med = S.media[ev.medium];
+                    float lsPdf = 1.f;                                   /* B5 */
+                    const float3 sp = hit.point, sn = hit.nS;            /* B7 */
+                    const LRef lsLight = sample_light(hit.point, hit.nS, &lsPdf);
+                    float3 lsPoint, lsNormal = mk(0.f, 0.f, 0.f);
+                    const Spec<NS> lsLe = sample_point(lsLight, ev, hit, lsPoint, lsNormal, lsPdf);
+                    const int choice = (rng.next() > 0.5f) ? 0 : 1;
+                    float distT, distPdf, eqT, eqPdf;
+                    const Spec<NS> mTrD = medium_sample_distance<NS>(med, rng, ev, hit, &distT, &distPdf);
+                    const bool intD = ev.mediumInteraction;
+                    const Spec<NS> mTrE = medium_sample_equiangular<NS>(med, ro, rd, rng, ev, hit, lsPoint, &eqT, &eqPdf);
+                    const bool intE = ev.mediumInteraction;
+                    ev.mediumInteraction = intD && intE;
+                    if (!ev.mediumInteraction) beta *= mTrD;
+                    if (ev.mediumInteraction) {
+                        ev.wo = -rd;
+                        Spec<NS> Ld(0.f);
+                        const float3 mpD = ro + rd * distT, mpE = ro + rd * eqT;
+                        const float distPdf2 = medium_pdf_distance<NS>(med, eqT);
+                        const float eqPdf2 = medium_pdf_equiangular(ro, rd, lsPoint, hit.tFar, distT);
+                        const float distW = power_heuristic(distPdf, eqPdf2);
+                        const float eqW = power_heuristic(eqPdf, distPdf2);
+                        float3 wiD, wiE;
+                        const Spec<NS> liD = ld_medium_point(ev, hit, mpD, lsLight, lsPoint, lsNormal, lsLe, lsPdf, wiD, sp, sn);
+                        Ld += liD * mTrD * distW;
+                        const Spec<NS> liE = ld_medium_point(ev, hit, mpE, lsLight, lsPoint, lsNormal, lsLe, lsPdf, wiE, sp, sn);
+                        Ld += liE * mTrE * eqW;
+                        ro = choice == 0 ? mpD : mpE;
+                        rd = choice == 0 ? wiD : wiE;
+                        scatterIntersect = intersect(ro, rd, hit);
+                        L += Ld;
+                        beta *= (choice == 0 ? mTrD : mTrE);
+                    }
+                } else ev.mediumInteraction = false;
+
+                if (!ev.mediumInteraction) {
+                    const DMaterial &m = mat(hit);
+                    if (m.has_bsdf) {
+                        ev.wo = -rd;
+                        ev.woL = ev_local(hit, ev.wo);
+                        ev.wiL = ev_local(hit, ev.wi);
+                        ev.sidedness = (ev.woL.y > 0.f) ? 1 : -1;
+                        Bsdf<NS> b;
+                        setup_bsdf(b, m, ev, hit);
+                        float lightDistPdf = 1.f;
+                        const float3 sp = hit.point, sn = hit.nS;   /* B7 */
+                        const LRef l = sample_light(hit.point, hit.nS, &lightDistPdf);
+                        Spec<NS> Ld(0.f);
+                        float scatteringPDF = 0.f, lightPDF = 0.f;
+                        Spec<NS> Li = sample_li(l, ev, hit, lightPDF);
+                        Spec<NS> f;
+                        lightPDF *= lightDistPdf;
+                        if (lightPDF > 0.f && !Li.black()) {
+                            f = bsdf_f<NS>(b, ev) * fabsf(ev.wiL.y);
+                            scatteringPDF = bsdf_pdf<NS>(b, ev.woL, ev.wiL);
+                            if (!f.black() && scatteringPDF > 0.f) {
+                                const float w = power_heuristic(lightPDF, scatteringPDF);
+                                Ld += Li * f * w / lightPDF;
+                            }
+                        }
+                        f = bsdf_sample_node<NS>(b, 0, ev, hit, rng, scatteringPDF, 0);
+                        f *= fabsf(ev.wiL.y);
+                        ro = hit.point;
+                        rd = ev.wi;
+                        ev.medium = get_medium(m, ev.wi, hit.nG);
+                        scatterIntersect = intersect(ro, rd, hit);
+                        if (scatteringPDF > 0.f && !f.black()) {
+                            LRef nl; nl.light = scatterIntersect ? mat(hit).light : S.env_light; nl.tri = -1;
+                            if (nl.light >= 0) {
+                                if (!lref_eq(nl, l)) lightDistPdf = light_pdf(sp, sn, hit.prim, nl);
+                                lightPDF = lightDistPdf * pdf_li(nl, ev, hit);
+                                Li = scatterIntersect ? light_L(nl, ev, hit) : light_Le(nl, rd);
+                                const float w = power_heuristic(scatteringPDF, lightPDF);
+                                if (!Li.black() && lightPDF > 0.f) Ld += Li * f * w / scatteringPDF;
+                            }
+                        } else break;
+                        L += beta * Ld;
+                        beta *= f / scatteringPDF;
+                    } else {
+                        ev.medium = get_medium(m, rd, hit.nG);
+                        ro = hit.point + hit.nG * (dot(hit.nG, rd) < 0.f ? -SURFACE_EPSILON : SURFACE_EPSILON);
+                        if (bounces > 0) scatterIntersect = intersect(ro, rd, hit);
+                        if (++nullCrossings > 256) break;
+                        bounces--;
+                        continue;
+                    }
+                }
+                if (bounces > minBounces) {
+                    const float q = smax(.05f, 1.f - spec_y<NS>(beta, lam));
+                    if (rng.next() < q) break;
+                    beta /= 1.f - q;
+                }
+            } else {
+                if (bounces == 0 && S.env_light >= 0) L += env_le(rd) * beta;
+                break;
+            }
+        }
+        return L;
+    }
+};
+
+}  // namespace lg

@@ -1,0 +1,42 @@
+/* Launch parameters shared by the API layer and the render kernels (internal). */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "lgpu_scene.h"
+
+namespace lg {
+
+struct CamParams {
+    float3 o, x, y, z;
+    float tanFov, tanFov2, aspect;
+    float xi, yi;   /* 1 / width, 1 / height */
+    int W, H;
+};
+struct RenderParams {
+    int spp, max_bounces, min_bounces;
+    uint32_t seed, sample_offset;
+};
+struct LaunchArgs {
+    DeviceScene S;
+    CamParams cam;
+    RenderParams rp;
+    float4 *film;
+    float4 *paths_out;
+    const uint64_t *ids;
+    uint64_t n;
+    unsigned long long *counters;
+    bool hero, count;
+    cudaStream_t stream;
+};
+
+cudaError_t launch_render_3_0(const LaunchArgs &a);
+cudaError_t launch_render_3_1(const LaunchArgs &a);
+cudaError_t launch_render_4_0(const LaunchArgs &a);
+cudaError_t launch_render_4_1(const LaunchArgs &a);
+inline cudaError_t launch_render(const LaunchArgs &a) {
+    if (a.hero) return a.count ? launch_render_4_1(a) : launch_render_4_0(a);
+    return a.count ? launch_render_3_1(a) : launch_render_3_0(a);
+}
+cudaError_t launch_intersect(const DeviceScene &S, const float *rays, uint32_t *hits, float *uvs, uint64_t n, cudaStream_t s);
+
+}  // namespace lg

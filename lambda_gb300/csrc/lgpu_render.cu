@@ -1,0 +1,160 @@
+/*
+ * Render kernels: one thread per path sample, the whole MIS volumetric path in registers
+ * (TileRenderers::UniformSpp + MISVolumetricPathIntegrator::Li, src/render/Render.cpp:43-64).
+ *
+ * Path p = (y * width + x) * spp + s.  Consecutive threads trace consecutive samples of one pixel,
+ * so a warp usually shares a pixel (spp a multiple of 32): its 32 radiance values are reduced with
+ * warp shuffles and added to the film by one lane -- Film::AddSample (src/camera/Film.h:30-33)
+ * without per-sample atomics.  Other warps fall back to per-lane float atomics.
+ */
+#include <cuda_runtime.h>
+
+#include "lgpu_integrator.cuh"
+#include "lgpu_launch.h"
+
+#ifndef LGPU_NS
+#define LGPU_NS 3
+#endif
+#ifndef LGPU_COUNT
+#define LGPU_COUNT 0
+#endif
+
+namespace lg {
+
+template <int NS>
+__device__ __forceinline__ void hero_to_rgb(const Spec<NS> &L, const Lambda4 &lam, float out[3]) {
+    if (NS == 3) { out[0] = L.c[0]; out[1] = L.c[1]; out[2] = L.c[2]; return; }
+    float xyz[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float w = L.c[i] * (HERO_RANGE / (4.0f * LGPU_CIE_Y_INTEGRAL));
+        xyz[0] += w * cie_at(d_cie_x, lam.l[i]);
+        xyz[1] += w * cie_at(d_cie_y, lam.l[i]);
+        xyz[2] += w * cie_at(d_cie_z, lam.l[i]);
+    }
+    out[0] = 3.240479f * xyz[0] - 1.537150f * xyz[1] - 0.498535f * xyz[2];
+    out[1] = -0.969256f * xyz[0] + 1.875991f * xyz[1] + 0.041556f * xyz[2];
+    out[2] = 0.055648f * xyz[0] - 0.204043f * xyz[1] + 1.057311f * xyz[2];
+}
+
+template <int NS, bool COUNT>
+__global__ void __launch_bounds__(128) k_render(DeviceScene S, CamParams cam, RenderParams rp, float4 *film,
+                                                float4 *paths_out, const uint64_t *ids, uint64_t n,
+                                                unsigned long long *counters) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < n;
+    float rgb[3] = {0.f, 0.f, 0.f};
+    uint32_t pixel = 0xffffffffu;
+    TravStats st = {0u, 0u, 0u};
+    if (active) {
+        const uint64_t pid = ids ? ids[i] : i;
+        pixel = (uint32_t)(pid / (uint64_t)rp.spp);
+        const uint32_t sidx = (uint32_t)(pid % (uint64_t)rp.spp) + rp.sample_offset;
+        const uint32_t x = pixel % (uint32_t)cam.W, y = pixel / (uint32_t)cam.W;
+        Rng rng;
+        rng.key = lgpu_path_key(rp.seed, pixel, sidx);
+        rng.dim = 0;
+        Lambda4 lam;
+        if (NS == 4) {
+            const float u = lgpu_rng_float(rng.key, LGPU_DIM_WAVELENGTH);
+            const float l0 = 380.0f + HERO_RANGE * u;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float l = l0 + (float)k * (HERO_RANGE / 4.0f);
+                if (l >= 720.0f) l -= HERO_RANGE;
+                lam.l[k] = l;
+            }
+        }
+        /* pixel jitter (Render.cpp:55-56) and PinholeCamera::GenerateRay (Camera.cpp:41-44) */
+        const float u = cam.xi * ((float)x + rng.next() - .5f);
+        const float v = cam.yi * ((float)y + rng.next() - .5f);
+        const float3 p = cam.o + cam.x * (u * -cam.tanFov2 + cam.tanFov) +
+                         cam.y * (v * -cam.tanFov2 * cam.aspect + cam.tanFov * cam.aspect) + cam.z;
+        const float3 d = normalised(p - cam.o);
+        Tracer<NS, COUNT> T{S, rng, lam, &st};
+        const Spec<NS> L = T.Li(cam.o, d, rp.max_bounces, rp.min_bounces);
+        hero_to_rgb<NS>(L, lam, rgb);
+        if (paths_out) paths_out[i] = make_float4(rgb[0], rgb[1], rgb[2], 0.f);
+    }
+    if (COUNT) {
+        const unsigned long long a = __reduce_add_sync(0xffffffffu, st.nodes);
+        const unsigned long long b = __reduce_add_sync(0xffffffffu, st.tris);
+        const unsigned long long c = __reduce_add_sync(0xffffffffu, st.rays);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&counters[0], a);
+            atomicAdd(&counters[1], b);
+            atomicAdd(&counters[2], c);
+        }
+    }
+    if (!film) return;
+    const unsigned full = 0xffffffffu;
+    const unsigned peers = __match_any_sync(full, pixel);
+    if (peers == full && active) {
+        float r = rgb[0], g = rgb[1], b = rgb[2];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            r += __shfl_down_sync(full, r, off);
+            g += __shfl_down_sync(full, g, off);
+            b += __shfl_down_sync(full, b, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            float *f = reinterpret_cast<float *>(&film[pixel]);
+            atomicAdd(f + 0, r);
+            atomicAdd(f + 1, g);
+            atomicAdd(f + 2, b);
+            atomicAdd(f + 3, 32.f);
+        }
+    } else if (active) {
+        float *f = reinterpret_cast<float *>(&film[pixel]);
+        atomicAdd(f + 0, rgb[0]);
+        atomicAdd(f + 1, rgb[1]);
+        atomicAdd(f + 2, rgb[2]);
+        atomicAdd(f + 3, 1.f);
+    }
+}
+
+#if LGPU_NS == 3 && LGPU_COUNT == 0
+/* Closest-hit queries for a ray batch (Scene::Intersect restated; tnear = 0, tfar = inf). */
+__global__ void k_intersect(DeviceScene S, const float4 *rays, uint4 *hits, float2 *uvs, uint64_t n) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = rays[2 * i], b = rays[2 * i + 1];
+    HitRec hr;
+    TravStats st;
+    const bool h = traverse<false>(S, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), b.w, false, &hr, &st);
+    if (h) {
+        hits[i] = make_uint4(__float_as_uint(hr.t), (unsigned)hr.prim, (unsigned)hr.obj, 0u);
+        if (uvs) uvs[i] = make_float2(hr.u, hr.v);
+    } else {
+        hits[i] = make_uint4(__float_as_uint(finf()), 0xffffffffu, 0xffffffffu, 0u);
+        if (uvs) uvs[i] = make_float2(0.f, 0.f);
+    }
+}
+#endif
+
+/* Each (spectral mode, counter) variant is compiled in its own translation unit so the four
+ * megakernel instantiations build in parallel: LGPU_NS and LGPU_COUNT select the variant. */
+#define LG_CAT2(a, b, c) a##b##_##c
+#define LG_CAT(a, b, c) LG_CAT2(a, b, c)
+
+cudaError_t LG_CAT(launch_render_, LGPU_NS, LGPU_COUNT)(const LaunchArgs &a) {
+    const int bs = 128;
+    const uint64_t blocks = (a.n + bs - 1) / bs;
+    if (blocks == 0) return cudaSuccess;
+    k_render<LGPU_NS, LGPU_COUNT != 0><<<(unsigned)blocks, bs, 0, a.stream>>>(a.S, a.cam, a.rp, a.film, a.paths_out, a.ids,
+                                                                            a.n, a.counters);
+    return cudaGetLastError();
+}
+
+#if LGPU_NS == 3 && LGPU_COUNT == 0
+cudaError_t launch_intersect(const DeviceScene &S, const float *rays, uint32_t *hits, float *uvs, uint64_t n, cudaStream_t s) {
+    const int bs = 128;
+    const uint64_t blocks = (n + bs - 1) / bs;
+    if (blocks == 0) return cudaSuccess;
+    k_intersect<<<(unsigned)blocks, bs, 0, s>>>(S, reinterpret_cast<const float4 *>(rays), reinterpret_cast<uint4 *>(hits),
+                                                reinterpret_cast<float2 *>(uvs), n);
+    return cudaGetLastError();
+}
+#endif
+
+}  // namespace lg

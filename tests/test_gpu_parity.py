@@ -1,0 +1,71 @@
+"""GPU path vs CPU oracle on the same seeded inputs (per path, per ray, per image).
+
+Criteria (from the reference's integrator run with the same counter-based RNG):
+  * per-path radiance within 1e-4 relative on >= 99 % of paths; the rest are divergences where a
+    1-ulp difference (FMA contraction on the GPU) flips a sampling decision;
+  * closest-hit primitive ids agree on >= 99.99 % of rays and t within 1e-5 relative;
+  * images: per-pixel means agree within a 3-sigma band of the per-pixel sample variance.
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from tests.parity import path_agreement, sample_ids
+
+pytestmark = pytest.mark.gpu
+
+
+def _render_both(lg, sb, cam, opts, n):
+    ids = sample_ids(opts, n)
+    r = lg.Renderer(sb)
+    g = r.render_paths(cam, opts, ids)
+    o = Oracle(sb).render_paths(cam, opts, ids)
+    r.close()
+    return g, o
+
+
+def test_cornell_rgb_paths(gpu_lib):
+    from lambda_gb300 import configs
+    sb, cam, opts = configs.cornell(48, 48, 4)
+    g, o = _render_both(gpu_lib, sb, cam, opts, 48 * 48 * 4)
+    frac, ok = path_agreement(g, o)
+    assert np.isfinite(g).all()
+    assert frac >= 0.99, "per-path agreement %.5f" % frac
+
+
+def test_cornell_hero_paths(gpu_lib):
+    from lambda_gb300 import abi, configs
+    sb, cam, opts = configs.cornell(32, 32, 4)
+    opts.spectral_mode = abi.SPECTRAL_HERO4
+    g, o = _render_both(gpu_lib, sb, cam, opts, 32 * 32 * 4)
+    frac, _ = path_agreement(g, o)
+    assert frac >= 0.99, "per-path agreement %.5f" % frac
+
+
+def test_terrain_small_paths(gpu_lib):
+    from lambda_gb300 import configs
+    sb, cam, opts = configs.terrain(64, 36, 4, grid=96, n_emitters=300)
+    g, o = _render_both(gpu_lib, sb, cam, opts, 64 * 36 * 4)
+    frac, _ = path_agreement(g, o)
+    assert frac >= 0.99, "per-path agreement %.5f" % frac
+
+
+def test_volume_small_paths(gpu_lib):
+    from lambda_gb300 import configs
+    sb, cam, opts = configs.volume(48, 27, 4, max_depth=12, n_instances=40, sphere_res=(24, 24))
+    g, o = _render_both(gpu_lib, sb, cam, opts, 48 * 27 * 4)
+    frac, _ = path_agreement(g, o)
+    assert frac >= 0.99, "per-path agreement %.5f" % frac
+
+
+def test_film_matches_paths(gpu_lib):
+    """lgpu_render's film equals the per-pixel sum of the per-path radiance."""
+    from lambda_gb300 import configs
+    sb, cam, opts = configs.cornell(32, 32, 32)
+    r = gpu_lib.Renderer(sb)
+    film = r.render(cam, opts)
+    ids = np.arange(32 * 32 * 32, dtype=np.uint64)
+    p = r.render_paths(cam, opts, ids).reshape(32, 32, 32, 4)
+    r.close()
+    np.testing.assert_allclose(film[..., 3], 32.0)
+    np.testing.assert_allclose(film[..., :3], p[..., :3].sum(axis=2), rtol=1e-4, atol=1e-5)
