@@ -17,7 +17,7 @@ LIB_PATH = HERE / "_build" / "liblambda_gpu.so"
 
 EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_scene_commit", "lgpu_render",
            "lgpu_render_device", "lgpu_render_paths", "lgpu_render_count", "lgpu_intersect",
-           "lgpu_get_stats", "lgpu_version"]
+           "lgpu_get_stats", "lgpu_version", "lgpu_scene_check"]
 
 _lib = None
 
@@ -54,8 +54,17 @@ def lib():
         L.lgpu_intersect.argtypes = [vp, vp, vp, vp, C.c_uint64, vp]
         L.lgpu_get_stats.argtypes = [vp, C.POINTER(abi.Stats)]
         L.lgpu_version.restype = C.c_char_p
+        L.lgpu_scene_check.argtypes = [C.POINTER(abi.SceneDesc), C.c_char_p, C.c_size_t]
         _lib = L
     return _lib
+
+
+def scene_check(scene):
+    """Compile + validate a scene on the host only (no GPU): returns (status, report)."""
+    desc = scene.desc()
+    buf = C.create_string_buffer(512)
+    rc = lib().lgpu_scene_check(C.byref(desc), buf, 512)
+    return rc, buf.value.decode()
 
 
 def _ptr(a):

@@ -95,6 +95,157 @@ void inverse3(const float *m, float *inv) {   /* column-major 3x3 inverse in dou
 
 inline lt::V3f v3(const float *p) { lt::V3f r; r.x = p[0]; r.y = p[1]; r.z = p[2]; return r; }
 
+/* Host-side image of the device scene: compile_scene fills it without touching the GPU,
+ * validate_scene checks every index a kernel will follow, lgpu_scene_commit uploads it. */
+struct HostScene {
+    DeviceScene S;
+    std::vector<DNode> nodes;
+    std::vector<DTri> tris;
+    std::vector<DInst> insts;
+    std::vector<DObject> objects;
+    std::vector<DMesh> meshes;
+    std::vector<float4> pos, nrm, tan;
+    std::vector<float2> uv;
+    std::vector<uint4> tri_idx;
+    std::vector<DMaterial> mats;
+    std::vector<DIns> code;
+    std::vector<DLight> lights;
+    std::vector<DLNode> lnodes;
+    std::vector<int2> treeLights, treeSlot;
+    std::vector<int> lightSlot;
+    std::vector<float> fpool;
+    std::vector<float4> envTex;
+    std::vector<DMedium> media;
+};
+
+int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H);
+
+bool check_ref(const HostScene &H, int ref, bool tlas, std::string &why) {
+    const int idx = ref >> 4, cnt = ref & 15;
+    if (idx < 0) { why = "negative child ref"; return false; }
+    if (cnt == 0) { if ((size_t)idx >= H.nodes.size()) { why = "node ref out of range"; return false; } return true; }
+    const size_t lim = tlas ? H.insts.size() : H.tris.size();
+    if ((size_t)idx + cnt > lim) { why = tlas ? "instance leaf out of range" : "triangle leaf out of range"; return false; }
+    return true;
+}
+
+/* Walk every BVH (TLAS and each BLAS) from its root; check refs, depth and leaf ranges. */
+bool check_bvh(const HostScene &H, int root, bool tlas, std::string &why) {
+    std::vector<std::pair<int, int>> st;   /* (ref, depth) */
+    st.push_back({root, 0});
+    size_t visits = 0;
+    while (!st.empty()) {
+        auto e = st.back();
+        st.pop_back();
+        if (++visits > 4 * (H.nodes.size() + H.tris.size() + H.insts.size() + 4)) { why = "BVH has a cycle"; return false; }
+        if (!check_ref(H, e.first, tlas, why)) return false;
+        if (e.second > LGPU_STACK - 8) { why = "BVH deeper than the traversal stack"; return false; }
+        const int idx = e.first >> 4, cnt = e.first & 15;
+        if (cnt == 0) {
+            const DNode &n = H.nodes[idx];
+            st.push_back({n.ch.x, e.second + 1});
+            st.push_back({n.ch.y, e.second + 1});
+        } else if (tlas) {
+            for (int k = 0; k < cnt; ++k) {
+                const DInst &I = H.insts[idx + k];
+                if (I.object >= (int)H.objects.size()) { why = "instance object out of range"; return false; }
+                if (!check_bvh(H, I.root, false, why)) return false;
+            }
+        } else {
+            for (int k = 0; k < cnt; ++k) {
+                const DTri &T = H.tris[idx + k];
+                int prim, obj;
+                std::memcpy(&prim, &T.v0.w, 4);
+                std::memcpy(&obj, &T.e1.w, 4);
+                if (obj >= (int)H.objects.size()) { why = "triangle object out of range"; return false; }
+                if (prim < 0) { why = "negative primitive id"; return false; }
+            }
+        }
+    }
+    return true;
+}
+
+bool check_prog(const HostScene &H, int off, int len, std::string &why) {
+    if (off < 0 || len < 0 || (size_t)off + len > H.code.size()) { why = "program range"; return false; }
+    for (int i = 0; i < len; ++i) {
+        const DIns &in = H.code[off + i];
+        if (in.op >= OP_COUNT) { why = "bad opcode"; return false; }
+        if (in.dst >= LGPU_MAX_REGS || in.a >= LGPU_MAX_REGS || in.b >= LGPU_MAX_REGS || in.c >= LGPU_MAX_REGS) { why = "register index"; return false; }
+        if (in.op == OP_MERGE && in.sub != 255 && in.sub >= LGPU_MAX_REGS) { why = "merge register"; return false; }
+    }
+    return true;
+}
+
+bool validate_scene(const HostScene &H, std::string &why) {
+    const DeviceScene &S = H.S;
+    if (!check_bvh(H, S.root, S.use_tlas != 0, why)) return false;
+    const size_t fp = H.fpool.size();
+    for (size_t i = 0; i < H.objects.size(); ++i) {
+        const DObject &o = H.objects[i];
+        if (o.mesh < 0 || (size_t)o.mesh >= H.meshes.size() || o.material < 0 || (size_t)o.material >= H.mats.size()) { why = "object refs"; return false; }
+    }
+    for (size_t i = 0; i < H.meshes.size(); ++i) {
+        const DMesh &m = H.meshes[i];
+        if ((size_t)m.tri_off + m.num_tris > H.tri_idx.size()) { why = "mesh triangle range"; return false; }
+        const size_t nv = (i + 1 < H.meshes.size() ? (size_t)H.meshes[i + 1].vtx_off : H.pos.size()) - m.vtx_off;
+        for (int t = 0; t < m.num_tris; ++t) {
+            const uint4 ti = H.tri_idx[m.tri_off + t];
+            if (ti.x >= nv || ti.y >= nv || ti.z >= nv) { why = "vertex index"; return false; }
+        }
+    }
+    if (H.nrm.size() != H.pos.size() || H.tan.size() != H.pos.size() || H.uv.size() != H.pos.size()) { why = "attribute sizes"; return false; }
+    for (const DMaterial &m : H.mats) {
+        if (m.light >= (int)H.lights.size() || m.medium_interior >= (int)H.media.size() || m.medium_exterior >= (int)H.media.size()) { why = "material refs"; return false; }
+        if (!m.has_bsdf) continue;
+        if (!check_prog(H, m.prog_off, m.prog_len, why)) return false;
+        if (m.num_leaves < 1 || m.num_leaves > LGPU_MAX_LEAVES || m.num_tree < 1 || m.num_tree > 2 * LGPU_MAX_LEAVES - 1) { why = "bsdf tree size"; return false; }
+        for (int k = 0; k < m.num_leaves; ++k)
+            if (m.leaves[k].albedo >= LGPU_MAX_REGS || m.leaves[k].rough >= LGPU_MAX_REGS) { why = "leaf register"; return false; }
+        for (int k = 0; k < m.num_tree; ++k) {
+            const DBsdfNode &n = m.tree[k];
+            if (n.kind == 0 && n.a >= m.num_leaves) { why = "bsdf leaf ref"; return false; }
+            if (n.kind == 1 && (n.a >= m.num_tree || n.b >= m.num_tree || n.ratio >= LGPU_MAX_REGS)) { why = "bsdf mix ref"; return false; }
+        }
+    }
+    const int ntl = (int)H.treeSlot.size();
+    for (const DLight &L : H.lights) {
+        if (L.type != LT_ENV) {
+            if (!check_prog(H, L.prog_off, L.prog_len, why)) return false;
+            if (L.out_reg < 0 || L.out_reg + 1 >= LGPU_MAX_REGS) { why = "emission register"; return false; }
+        }
+        if (L.type == LT_MESH) {
+            if (L.object < 0 || (size_t)L.object >= H.objects.size()) { why = "mesh light object"; return false; }
+            if (L.dist_off < 0 || (size_t)L.dist_off + 2 * L.num_tris + 1 > fp) { why = "mesh light cdf"; return false; }
+            if (S.light_strategy == LGPU_LIGHT_STRATEGY_TREE && (L.tri_base < 0 || L.tri_base + L.num_tris > ntl)) { why = "mesh light tree base"; return false; }
+        }
+    }
+    if ((size_t)S.power_cdf_off + 2 * H.lights.size() + 1 > fp) { why = "power cdf"; return false; }
+    if (S.light_strategy == LGPU_LIGHT_STRATEGY_TREE && !H.lnodes.empty()) {
+        if (S.tree_root < 0 || (size_t)S.tree_root >= H.lnodes.size()) { why = "tree root"; return false; }
+        for (const DLNode &n : H.lnodes) {
+            if (n.child0 >= (int)H.lnodes.size() || n.child1 >= (int)H.lnodes.size() || n.parent >= (int)H.lnodes.size()) { why = "tree links"; return false; }
+            if ((n.child0 < 0) != (n.child1 < 0)) { why = "tree node with one child"; return false; }
+            if (n.first < 0 || n.num < 1 || n.first + n.num > (int)H.treeLights.size()) { why = "tree light range"; return false; }
+            if (n.child0 < 0 && (n.dist_off < 0 || (size_t)n.dist_off + 2 * n.num + 1 > fp)) { why = "tree leaf cdf"; return false; }
+        }
+        for (const int2 &t : H.treeLights)
+            if (t.x < 0 || (size_t)t.x >= H.lights.size() || t.y >= H.lights[t.x].num_tris + (H.lights[t.x].type == LT_MESH ? 0 : 1)) { why = "tree light ref"; return false; }
+        for (const int2 &t : H.treeSlot)
+            if (t.x < 0 || (size_t)t.x >= H.lnodes.size() || t.y < 0 || t.y >= H.lnodes[t.x].num) { why = "tree slot"; return false; }
+        for (size_t i = 0; i < H.lightSlot.size(); ++i) {
+            const int ls = H.lightSlot[i];
+            const int ty = H.lights[i].type;
+            if ((ty == LT_POINT || ty == LT_SPOT) && (ls < 0 || ls >= ntl)) { why = "light slot"; return false; }
+        }
+    }
+    if (S.env_light >= 0) {
+        const DEnv &E = S.env;
+        if ((size_t)E.tex_off + (size_t)E.w * E.h > H.envTex.size()) { why = "env texture"; return false; }
+        if ((size_t)E.cond_off + (size_t)E.h * (2 * E.w + 2) > fp || (size_t)E.marg_off + 2 * E.h + 1 > fp) { why = "env cdf"; return false; }
+    }
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -136,16 +287,40 @@ LGPU_API void lgpu_destroy(lgpu_context *c) {
 
 LGPU_API const char *lgpu_last_error(const lgpu_context *c) { return c ? c->err.c_str() : "null context"; }
 
+/* Compile and validate a scene on the host only (no CUDA call); writes a short report. */
+LGPU_API int lgpu_scene_check(const lgpu_scene_desc *d, char *report, size_t report_size) {
+    lgpu_context tmp;
+    HostScene H;
+    int rc = compile_scene(&tmp, d, H);
+    std::string msg;
+    if (rc == LGPU_OK) {
+        std::string why;
+        if (!validate_scene(H, why)) { rc = LGPU_ERR_INVALID_SCENE; msg = "validation: " + why; }
+        else {
+            msg = "ok nodes=" + std::to_string(H.nodes.size()) + " tris=" + std::to_string(H.tris.size()) +
+                  " insts=" + std::to_string(H.insts.size()) + " prog=" + std::to_string(H.code.size()) +
+                  " lnodes=" + std::to_string(H.lnodes.size()) + " fpool=" + std::to_string(H.fpool.size()) +
+                  " tree_power=" + std::to_string(H.S.tree_power);
+        }
+    } else msg = tmp.err;
+    if (report && report_size) {
+        std::strncpy(report, msg.c_str(), report_size - 1);
+        report[report_size - 1] = 0;
+    }
+    return rc;
+}
+
 LGPU_API int lgpu_get_stats(const lgpu_context *c, lgpu_stats *out) {
     if (!c || !out) return LGPU_ERR_INVALID_ARG;
     *out = c->stats;
     return LGPU_OK;
 }
 
-LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
-    if (!c || !d) return LGPU_ERR_INVALID_ARG;
-    cudaSetDevice(c->device);
-    free_scene(c);
+}  // extern "C"
+
+namespace {
+int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
+    if (!d) return LGPU_ERR_INVALID_ARG;
     /* ---------------- validation */
     for (int i = 0; i < d->num_objects; ++i) {
         const lgpu_object_desc &o = d->objects[i];
@@ -159,19 +334,19 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
     }
     if (d->num_lights == 0) return fail(c, LGPU_ERR_INVALID_SCENE, "scene has no light (the reference requires one)");
 
-    std::vector<float> fpool;
-    DeviceScene S;
+    std::vector<float> &fpool = H.fpool;
+    DeviceScene &S = H.S;
     std::memset(&S, 0, sizeof(S));
     S.has_volumes = d->has_volumes;
     S.light_strategy = d->light_strategy;
     S.num_lights = d->num_lights;
-    size_t bytes = 0;
 
     /* ---------------- meshes: vertex attributes */
-    std::vector<float4> pos, nrm, tan;
-    std::vector<float2> uv;
-    std::vector<uint4> tri_idx;
-    std::vector<DMesh> meshes(d->num_meshes);
+    std::vector<float4> &pos = H.pos, &nrm = H.nrm, &tan = H.tan;
+    std::vector<float2> &uv = H.uv;
+    std::vector<uint4> &tri_idx = H.tri_idx;
+    std::vector<DMesh> &meshes = H.meshes;
+    meshes.resize(d->num_meshes);
     for (int i = 0; i < d->num_meshes; ++i) {
         const lgpu_mesh_desc &m = d->meshes[i];
         DMesh &dm = meshes[i];
@@ -190,7 +365,8 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
     }
 
     /* ---------------- objects */
-    std::vector<DObject> objects(d->num_objects);
+    std::vector<DObject> &objects = H.objects;
+    objects.resize(d->num_objects);
     lt::Box sceneBox;
     bool firstBox = true;
     std::vector<lt::Box> objBox(d->num_objects);
@@ -229,9 +405,9 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
     }
 
     /* ---------------- geometry: BLAS / TLAS */
-    std::vector<DNode> nodes;
-    std::vector<DTri> tris;
-    std::vector<DInst> insts;
+    std::vector<DNode> &nodes = H.nodes;
+    std::vector<DTri> &tris = H.tris;
+    std::vector<DInst> &insts = H.insts;
     auto make_tri = [&](const lgpu_mesh_desc &m, uint32_t t, int objId) {
         const float *v0 = m.vertices + 3 * m.triangles[3 * t], *v1 = m.vertices + 3 * m.triangles[3 * t + 1], *v2 = m.vertices + 3 * m.triangles[3 * t + 2];
         DTri T;
@@ -339,11 +515,12 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
     if (maxDepth > LGPU_STACK - 4) return fail(c, LGPU_ERR_INVALID_SCENE, "BVH too deep for the traversal stack");
 
     /* ---------------- materials */
-    std::vector<DIns> code;
+    std::vector<DIns> &code = H.code;
     GraphCompiler gc;
     gc.d = d;
     gc.code = &code;
-    std::vector<DMaterial> mats(d->num_materials);
+    std::vector<DMaterial> &mats = H.mats;
+    mats.resize(d->num_materials);
     for (int i = 0; i < d->num_materials; ++i) {
         const lgpu_material_desc &md = d->materials[i];
         DMaterial &m = mats[i];
@@ -360,15 +537,17 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
     }
 
     /* ---------------- lights */
-    std::vector<DLight> lights(d->num_lights);
+    std::vector<DLight> &lights = H.lights;
+    lights.resize(d->num_lights);
     std::vector<lt::TreeLightIn> treeIn;
     std::vector<int2> treeRef;      /* (light, tri) per tree light, input order */
-    std::vector<int> lightSlot(d->num_lights, -1);
+    std::vector<int> &lightSlot = H.lightSlot;
+    lightSlot.assign(d->num_lights, -1);
     std::vector<float> lightPower(d->num_lights, 0.f);
     int envLight = -1;
     DEnv env;
     std::memset(&env, 0, sizeof(env));
-    std::vector<float4> envTex;
+    std::vector<float4> &envTex = H.envTex;
     const float PIf = 3.14159265358979323846f;
     for (int i = 0; i < d->num_lights; ++i) {
         const lgpu_light_desc &ld = d->lights[i];
@@ -521,8 +700,8 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
         S.power_integral = lt::piecewise1d(lightPower.data(), (unsigned)d->num_lights, fpool, S.power_cdf_off);
         S.inv_total_power = 1.f / tot;
     }
-    std::vector<int2> treeLights, treeSlot;
-    std::vector<DLNode> lnodes;
+    std::vector<int2> &treeLights = H.treeLights, &treeSlot = H.treeSlot;
+    std::vector<DLNode> &lnodes = H.lnodes;
     if (d->light_strategy == LGPU_LIGHT_STRATEGY_TREE) {
         lt::TreeOut to;
         lt::build_light_tree(treeIn, fpool, to);
@@ -551,7 +730,8 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
     }
 
     /* ---------------- media */
-    std::vector<DMedium> media(d->num_media);
+    std::vector<DMedium> &media = H.media;
+    media.resize(d->num_media);
     for (int i = 0; i < d->num_media; ++i) {
         DMedium &m = media[i];
         std::memset(&m, 0, sizeof(m));
@@ -559,6 +739,29 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
         m.g = d->media[i].g;
     }
 
+    return LGPU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
+    if (!c || !d) return LGPU_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    free_scene(c);
+    HostScene H;
+    int rc = compile_scene(c, d, H);
+    if (rc) return rc;
+    std::string why;
+    if (!validate_scene(H, why)) return fail(c, LGPU_ERR_INVALID_SCENE, "compiled scene failed validation: " + why);
+    DeviceScene S = H.S;
+    size_t bytes = 0;
+    const auto &nodes = H.nodes; const auto &tris = H.tris; const auto &insts = H.insts; const auto &objects = H.objects;
+    const auto &meshes = H.meshes; const auto &pos = H.pos; const auto &nrm = H.nrm; const auto &tan = H.tan;
+    const auto &uv = H.uv; const auto &tri_idx = H.tri_idx; const auto &mats = H.mats; const auto &code = H.code;
+    const auto &lights = H.lights; const auto &lnodes = H.lnodes; const auto &treeLights = H.treeLights;
+    const auto &treeSlot = H.treeSlot; const auto &lightSlot = H.lightSlot; const auto &fpool = H.fpool;
+    const auto &envTex = H.envTex; const auto &media = H.media;
     /* ---------------- upload */
     bool ok = upload(c, nodes, &S.nodes, bytes) && upload(c, tris, &S.tris, bytes) && upload(c, insts, &S.insts, bytes) &&
               upload(c, objects, &S.objects, bytes) && upload(c, meshes, &S.meshes, bytes) && upload(c, pos, &S.pos, bytes) &&

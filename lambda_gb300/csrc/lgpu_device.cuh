@@ -166,10 +166,11 @@ HD float voronoi2d(float u, float v, float scale) {
     for (int y = -1; y < 2; ++y)
         for (int x = -1; x < 2; ++x) {
             const float ox = px + (float)x, oy = py + (float)y;
-            const float hx = ox * 127.1f + oy * 311.7f, hy = ox * 269.5f + oy * 183.3f;
+            const float hx = add_rn(mul_rn(ox, 127.1f), mul_rn(oy, 311.7f));
+            const float hy = add_rn(mul_rn(ox, 269.5f), mul_rn(oy, 183.3f));
             const float sx = sinf(hx) * 18.5453f, sy = sinf(hy) * 18.5453f;
             const float rx = ox + fractf(sx) - u, ry = oy + fractf(sy) - v;
-            const float d2 = rx * rx + ry * ry;
+            const float d2 = add_rn(mul_rn(rx, rx), mul_rn(ry, ry));
             if (d2 < m) m = d2;
         }
     return sqrtf(m);
@@ -184,11 +185,11 @@ HD float voronoi3d(float3 p, float scale) {
             for (int x = -1; x < 2; ++x) {
                 const float3 off = b + mk((float)x, (float)y, (float)z);
                 float3 q = fract3(off * mk(.1031f, .1030f, .0973f));
-                const float d = dot(q, mk(q.y, q.x, q.z) + mk(33.33f, 33.33f, 33.33f));
+                const float d = add_rn(add_rn(mul_rn(q.x, q.y + 33.33f), mul_rn(q.y, q.x + 33.33f)), mul_rn(q.z, q.z + 33.33f));
                 q = q + mk(d, d, d);
                 const float3 hsh = fract3((mk(q.x, q.x, q.y) + mk(q.y, q.x, q.x)) * mk(q.z, q.y, q.z));
                 const float3 rp = off + hsh - p;
-                const float d2 = dot(rp, rp);
+                const float d2 = add_rn(add_rn(mul_rn(rp.x, rp.x), mul_rn(rp.y, rp.y)), mul_rn(rp.z, rp.z));
                 if (d2 < m) m = d2;
             }
     return sqrtf(m);
@@ -489,24 +490,38 @@ HD float leaf_pdf(const DLeaf &L, float rough, float3 wo, float3 wi) {
     default: return cos_hemi_pdf(wo, wi);
     }
 }
+/* Mix trees are at most two levels deep; the depth is a template parameter so no device function
+ * recurses (the stack size stays statically known). */
+template <int NS, int D>
+struct MixEval {
+    HD static Spec<NS> f(const Bsdf<NS> &b, int slot, const Event &ev) {
+        const DBsdfNode nd = b.m->tree[slot];
+        if (nd.kind == 0) return leaf_f<NS>(b.m->leaves[nd.a], b.alb[nd.a], b.rough[nd.a], ev);
+        const float r = b.ratio[slot];
+        return MixEval<NS, D + 1>::f(b, nd.a, ev) * (1.f - r) + MixEval<NS, D + 1>::f(b, nd.b, ev) * r;
+    }
+    HD static float pdf(const Bsdf<NS> &b, int slot, float3 wo, float3 wi) {
+        const DBsdfNode nd = b.m->tree[slot];
+        if (nd.kind == 0) return leaf_pdf(b.m->leaves[nd.a], b.rough[nd.a], wo, wi);
+        const float r = b.ratio[slot];
+        return MixEval<NS, D + 1>::pdf(b, nd.a, wo, wi) * (1.f - r) + MixEval<NS, D + 1>::pdf(b, nd.b, wo, wi) * r;
+    }
+};
 template <int NS>
-HD Spec<NS> bsdf_f_node(const Bsdf<NS> &b, int slot, const Event &ev, int depth) {
-    const DBsdfNode nd = b.m->tree[slot];
-    if (nd.kind == 0) return leaf_f<NS>(b.m->leaves[nd.a], b.alb[nd.a], b.rough[nd.a], ev);
-    if (depth >= 2) return Spec<NS>(0.f);
-    const float r = b.ratio[slot];
-    return bsdf_f_node<NS>(b, nd.a, ev, depth + 1) * (1.f - r) + bsdf_f_node<NS>(b, nd.b, ev, depth + 1) * r;
-}
-template <int NS>
-HD float bsdf_pdf_node(const Bsdf<NS> &b, int slot, float3 wo, float3 wi, int depth) {
-    const DBsdfNode nd = b.m->tree[slot];
-    if (nd.kind == 0) return leaf_pdf(b.m->leaves[nd.a], b.rough[nd.a], wo, wi);
-    if (depth >= 2) return 0.f;
-    const float r = b.ratio[slot];
-    return bsdf_pdf_node<NS>(b, nd.a, wo, wi, depth + 1) * (1.f - r) + bsdf_pdf_node<NS>(b, nd.b, wo, wi, depth + 1) * r;
-}
-template <int NS> HD Spec<NS> bsdf_f(const Bsdf<NS> &b, const Event &ev) { return bsdf_f_node<NS>(b, 0, ev, 0); }
-template <int NS> HD float bsdf_pdf(const Bsdf<NS> &b, float3 wo, float3 wi) { return bsdf_pdf_node<NS>(b, 0, wo, wi, 0); }
+struct MixEval<NS, 3> {
+    HD static Spec<NS> f(const Bsdf<NS> &b, int slot, const Event &ev) {
+        const DBsdfNode nd = b.m->tree[slot];
+        if (nd.kind == 0) return leaf_f<NS>(b.m->leaves[nd.a], b.alb[nd.a], b.rough[nd.a], ev);
+        return Spec<NS>(0.f);
+    }
+    HD static float pdf(const Bsdf<NS> &b, int slot, float3 wo, float3 wi) {
+        const DBsdfNode nd = b.m->tree[slot];
+        if (nd.kind == 0) return leaf_pdf(b.m->leaves[nd.a], b.rough[nd.a], wo, wi);
+        return 0.f;
+    }
+};
+template <int NS> HD Spec<NS> bsdf_f(const Bsdf<NS> &b, const Event &ev) { return MixEval<NS, 0>::f(b, 0, ev); }
+template <int NS> HD float bsdf_pdf(const Bsdf<NS> &b, float3 wo, float3 wi) { return MixEval<NS, 0>::pdf(b, 0, wo, wi); }
 
 /* BxDF::Sample_f of one leaf; moves hit.point off the surface as each reference lobe does. */
 template <int NS>
@@ -577,19 +592,31 @@ HD Spec<NS> leaf_sample(const Bsdf<NS> &b, int li, Event &ev, RayHit &h, Rng &rn
     }
     }
 }
-/* MixBSDF::Sample_f (BxDF.cpp:51-60), recursive over the mix tree. */
+/* MixBSDF::Sample_f (BxDF.cpp:51-60) over the mix tree: descend choosing a child per level
+ * (one Get1D each), sample the leaf, then combine on the way up with the other children's f. */
 template <int NS>
-HD Spec<NS> bsdf_sample_node(const Bsdf<NS> &b, int slot, Event &ev, RayHit &h, Rng &rng, float &pdf, int depth) {
-    const DBsdfNode nd = b.m->tree[slot];
-    if (nd.kind == 0) return leaf_sample<NS>(b, nd.a, ev, h, rng, pdf);
-    if (depth >= 2) { pdf = 0.f; return Spec<NS>(0.f); }
-    const float r = b.ratio[slot];
-    if (rng.next() > r) {
-        const Spec<NS> af = bsdf_sample_node<NS>(b, nd.a, ev, h, rng, pdf, depth + 1);
-        return af * (1.f - r) + bsdf_f_node<NS>(b, nd.b, ev, depth + 1) * r;
+HD Spec<NS> bsdf_sample(const Bsdf<NS> &b, Event &ev, RayHit &h, Rng &rng, float &pdf) {
+    int path[3];
+    bool tookA[3];
+    int depth = 0;
+    int slot = 0;
+    while (b.m->tree[slot].kind == 1 && depth < 2) {
+        const DBsdfNode nd = b.m->tree[slot];
+        const bool a = rng.next() > b.ratio[slot];
+        path[depth] = slot;
+        tookA[depth] = a;
+        ++depth;
+        slot = a ? nd.a : nd.b;
     }
-    const Spec<NS> bf = bsdf_sample_node<NS>(b, nd.b, ev, h, rng, pdf, depth + 1);
-    return bf * r + bsdf_f_node<NS>(b, nd.a, ev, depth + 1) * (1.f - r);
+    if (b.m->tree[slot].kind == 1) { pdf = 0.f; return Spec<NS>(0.f); }
+    Spec<NS> v = leaf_sample<NS>(b, b.m->tree[slot].a, ev, h, rng, pdf);
+    for (int k = depth - 1; k >= 0; --k) {
+        const DBsdfNode nd = b.m->tree[path[k]];
+        const float r = b.ratio[path[k]];
+        if (tookA[k]) v = v * (1.f - r) + MixEval<NS, 1>::f(b, nd.b, ev) * r;
+        else v = v * r + MixEval<NS, 1>::f(b, nd.a, ev) * (1.f - r);
+    }
+    return v;
 }
 
 /* ------------------------------------------------------------------ media */

@@ -251,6 +251,7 @@ struct Tracer {
         const DLight &L = S.lights[r.light];
         if (L.type == LT_ENV) return env_pdf_li(ev);
         if (L.type != LT_MESH) return 0.f;
+        if (h.prim >= L.num_tris) return 0.f;   /* hit object does not carry this light's mesh */
         if (dot(ev.wi, h.nG) > 0.f) return 0.f;
         const float distSq = h.tFar * h.tFar;
         float3 a, b, c;
@@ -399,8 +400,12 @@ struct Tracer {
         if (S.light_strategy == LGPU_LIGHT_STRATEGY_POWER) return L.power * S.inv_total_power;
         if (L.type == LT_ENV) return S.inf_power / (S.inf_power + S.tree_power);
         int ti;
-        if (L.type == LT_MESH) ti = L.tri_base + (l.tri >= 0 ? l.tri : prim);
-        else ti = S.light_slot[l.light];
+        if (L.type == LT_MESH) {
+            const int t = l.tri >= 0 ? l.tri : prim;
+            if (t < 0 || t >= L.num_tris) return 0.f;
+            ti = L.tri_base + t;
+        } else ti = S.light_slot[l.light];
+        if (ti < 0 || ti >= S.num_tree_lights) return 0.f;
         const int2 slot = __ldg(&S.tree_slot[ti]);
         const DLNode &leaf = S.lnodes[slot.x];
         const float pdf = S.fpool[leaf.dist_off + leaf.num + 1 + slot.y];   /* raw power (Piecewise1D::PDF) */
@@ -561,7 +566,7 @@ struct Tracer {
                                 Ld += Li * f * w / lightPDF;
                             }
                         }
-                        f = bsdf_sample_node<NS>(b, 0, ev, hit, rng, scatteringPDF, 0);
+                        f = bsdf_sample<NS>(b, ev, hit, rng, scatteringPDF);
                         f *= fabsf(ev.wiL.y);
                         ro = hit.point;
                         rd = ev.wi;

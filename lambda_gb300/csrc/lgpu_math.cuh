@@ -36,6 +36,15 @@ HD float smax(float a, float b) { return (a < b) ? b : a; }
 HD float smin(float a, float b) { return (b < a) ? b : a; }
 HD float clampr(float v, float lo, float hi) { return smax(smin(v, hi), lo); }
 HD float lerpf(float a, float b, float r) { return a + (b - a) * r; }
+/* Separately rounded multiply / add: no FMA contraction, so sensitive expressions (noise hashes
+ * that feed sin() at large arguments) round exactly like the CPU restatement. */
+#if defined(__CUDA_ARCH__)
+HD float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+HD float add_rn(float a, float b) { return __fadd_rn(a, b); }
+#else
+HD float mul_rn(float a, float b) { return a * b; }
+HD float add_rn(float a, float b) { return a + b; }
+#endif
 HD float fractf(float r) { return r - floorf(r); }
 
 HD float3 mk(float x, float y, float z) { return make_float3(x, y, z); }

@@ -74,7 +74,8 @@ __global__ void __launch_bounds__(128) k_render(DeviceScene S, CamParams cam, Re
         Tracer<NS, COUNT> T{S, rng, lam, &st};
         const Spec<NS> L = T.Li(cam.o, d, rp.max_bounces, rp.min_bounces);
         hero_to_rgb<NS>(L, lam, rgb);
-        if (paths_out) paths_out[i] = make_float4(rgb[0], rgb[1], rgb[2], 0.f);
+        /* w = random numbers drawn: a control-flow fingerprint of the path */
+        if (paths_out) paths_out[i] = make_float4(rgb[0], rgb[1], rgb[2], (float)rng.dim);
     }
     if (COUNT) {
         const unsigned long long a = __reduce_add_sync(0xffffffffu, st.nodes);

@@ -58,11 +58,11 @@ struct DMesh {
     int flags;      /* 1 = smooth normals+tangents, 2 = uvs */
 };
 
-/* Bytecode instruction.  dst/a/b/c are register indices, k are immediates. */
+/* Bytecode instruction (24 bytes).  dst/a/b/c are register indices, k are immediates. */
 struct DIns {
     uint8_t op, dst, a, b;
     uint8_t c, sub, pad0, pad1;
-    float k[2];
+    float k[4];
 };
 
 /* BSDF tree of one material: up to 4 leaves under up to 3 Mix nodes.

@@ -2212,7 +2212,7 @@ static void SetWavelengths(uint32_t key) {
 }
 
 /* One path: pixel jitter (Render.cpp:55-56), pinhole ray (Camera.cpp:41-44), Li. */
-static Spec TracePath(const OracleRun &R, uint64_t pathId, Real rgbOut[3]) {
+static Spec TracePath(const OracleRun &R, uint64_t pathId, Real rgbOut[3], uint32_t *dimsOut) {
     const int W = R.opt->width, H = R.opt->height, spp = R.opt->spp;
     const uint32_t pixel = (uint32_t)(pathId / (uint64_t)spp);
     const uint32_t sIdx = (uint32_t)(pathId % (uint64_t)spp) + R.opt->sample_offset;
@@ -2234,6 +2234,7 @@ static Spec TracePath(const OracleRun &R, uint64_t pathId, Real rgbOut[3]) {
     Ray r{org, (p - org).Normalised()};
     Integrator I(R.o->sc, R.opt->max_bounces, R.opt->min_bounces);
     const Spec L = I.Li(r, s);
+    if (dimsOut) *dimsOut = s.dim;
     if (g_ns == 3) { rgbOut[0] = L.c[0]; rgbOut[1] = L.c[1]; rgbOut[2] = L.c[2]; }
     else {
         Real xyz[3] = {0, 0, 0};
@@ -2256,6 +2257,14 @@ LGPU_API void *oracle_create(const lgpu_scene_desc *d) {
     return o;
 }
 LGPU_API void oracle_destroy(void *o) { delete (Oracle *)o; }
+/* Light-tree summary: total tree power, infinite-light power and number of tree lights. */
+LGPU_API void oracle_tree_info(void *h, float *out) {
+    Oracle *o = (Oracle *)h;
+    out[0] = out[1] = out[2] = 0;
+    if (auto *t = dynamic_cast<TreeSamplerO *>(o->sc.lightSampler.get())) {
+        out[0] = t->treePower; out[1] = t->infPower; out[2] = (float)t->lights.size();
+    }
+}
 
 /* Render paths [n ids or, when ids == NULL, every path of the frame].  film (optional) receives
  * summed RGB + count per pixel; path_out (optional) receives RGB + 0 per listed path. */
@@ -2277,8 +2286,9 @@ LGPU_API int oracle_render(void *handle, const lgpu_camera_desc *cam, const lgpu
             for (uint64_t i = b; i < e; ++i) {
                 const uint64_t pid = ids ? ids[i] : i;
                 Real rgb[3];
-                TracePath(R, pid, rgb);
-                if (path_out) { path_out[4 * i] = rgb[0]; path_out[4 * i + 1] = rgb[1]; path_out[4 * i + 2] = rgb[2]; path_out[4 * i + 3] = 0; }
+                uint32_t dims = 0;
+                TracePath(R, pid, rgb, &dims);
+                if (path_out) { path_out[4 * i] = rgb[0]; path_out[4 * i + 1] = rgb[1]; path_out[4 * i + 2] = rgb[2]; path_out[4 * i + 3] = (float)dims; }
                 if (film) {
                     const uint64_t px = pid / (uint64_t)opt->spp;
                     float *f = &(*acc)[4 * px];

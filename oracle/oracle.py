@@ -65,6 +65,7 @@ def lib():
         L.oracle_cone_union.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_momega.restype = C.c_float
         L.oracle_momega.argtypes = [C.c_float, C.c_float]
+        L.oracle_tree_info.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_rng_bits.restype = C.c_uint32
         L.oracle_rng_bits.argtypes = [C.c_uint32] * 4
         _lib = L
@@ -105,6 +106,11 @@ class Oracle:
         cam = camera.desc()
         lib().oracle_render(self._h, C.byref(cam), C.byref(opts), _p(ids), len(ids), None, _p(outp), threads)
         return outp
+
+    def tree_info(self):
+        out = np.zeros(3, np.float32)
+        lib().oracle_tree_info(self._h, _p(out))
+        return {"tree_power": float(out[0]), "inf_power": float(out[1]), "tree_lights": int(out[2])}
 
     def intersect(self, o, d):
         ray = np.array(list(o) + [0.0] + list(d) + [np.inf], np.float32)

@@ -1,0 +1,56 @@
+"""Host-side scene compilation (no GPU): the compiled device scene passes index validation and the
+light tree matches the oracle's ManyLightSampler build."""
+import re
+
+import pytest
+
+from lambda_gb300 import configs
+
+
+@pytest.fixture(scope="module")
+def lg():
+    import lambda_gb300 as lg
+    lg.build()
+    return lg
+
+
+CASES = {
+    "cornell": lambda: configs.cornell(32, 32, 4),
+    "terrain_small": lambda: configs.terrain(64, 36, 4, grid=96, n_emitters=300),
+    "volume_small": lambda: configs.volume(48, 27, 4, n_instances=40, sphere_res=(24, 24)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_scene_compiles_and_validates(lg, name):
+    sb, cam, opts = CASES[name]()
+    rc, rep = lg.scene_check(sb)
+    assert rc == 0, rep
+    assert rep.startswith("ok"), rep
+
+
+@pytest.mark.parametrize("name", ["cornell", "terrain_small", "volume_small"])
+def test_light_tree_power_matches_oracle(lg, name):
+    from oracle.oracle import Oracle
+    sb, cam, opts = CASES[name]()
+    rc, rep = lg.scene_check(sb)
+    assert rc == 0, rep
+    tp = float(re.search(r"tree_power=([0-9.eE+-]+)", rep).group(1))
+    info = Oracle(sb).tree_info()
+    assert tp == pytest.approx(info["tree_power"], rel=1e-6)
+
+
+def test_bad_scene_rejected(lg):
+    sb, cam, opts = configs.cornell(8, 8, 1)
+    sb.objects[0] = (sb.objects[0][0], sb.objects[0][1], 999, sb.objects[0][3])   # material out of range
+    rc, rep = lg.scene_check(sb)
+    assert rc != 0 and "material" in rep
+
+
+def test_unsupported_node_rejected(lg):
+    sb, cam, opts = configs.cornell(8, 8, 1)
+    tex = sb.node("IMAGE_TEXTURE")
+    bx = sb.node("BXDF_LAMBERTIAN", inputs={0: lg.out(tex)})
+    sb.materials[0] = (bx, -1, -1, -1)
+    rc, rep = lg.scene_check(sb)
+    assert rc != 0 and "unsupported" in rep
