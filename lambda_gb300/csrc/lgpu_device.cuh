@@ -213,7 +213,7 @@ HD float noise3(int kind, float3 p, float scale) {
 
 /* Run one program: registers are float4; spectra occupy xyz (RGB3) or xyzw (HERO4). */
 template <int NS>
-HD void run_prog(const DIns *p, int n, const ShadeCtx &c, const Lambda4 &lam, float4 *R) {
+__host__ __device__ __noinline__ void run_prog(const DIns *p, int n, const ShadeCtx &c, const Lambda4 &lam, float4 *R) {
     for (int i = 0; i < n; ++i) {
         const DIns in = p[i];
         float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -743,7 +743,7 @@ __device__ __forceinline__ int4 ldg4i(const int4 *p) { return __ldg(p); }
 
 /* Closest hit (any_hit = false) or occlusion (any_hit = true) over TLAS + BLAS. */
 template <bool COUNT>
-__device__ bool traverse(const DeviceScene &S, float3 wo, float3 wd, float tmax, bool any_hit, HitRec *hr, TravStats *st) {
+__device__ __noinline__ bool traverse(const DeviceScene &S, float3 wo, float3 wd, float tmax, bool any_hit, HitRec *hr, TravStats *st) {
     int stack[LGPU_STACK];
     int sp = 0;
     stack[sp++] = S.root;   /* encoded child ref of the root */
@@ -819,7 +819,7 @@ __device__ bool traverse(const DeviceScene &S, float3 wo, float3 wd, float tmax,
 
 /* Object::Hit + TriangleMesh/Instance::ProcessHit (Object.h:27-35, TriangleMesh.cpp:80-114,
  * Instance.cpp:36-43); B18 transforms Ng, B26 uses the instance that was hit. */
-static __device__ __forceinline__ void process_hit(const DeviceScene &S, float3 o, float3 d, const HitRec &hr, RayHit &h) {
+static __device__ __noinline__ void process_hit(const DeviceScene &S, float3 o, float3 d, const HitRec &hr, RayHit &h) {
     const DObject &ob = S.objects[hr.obj];
     const DMesh me = S.meshes[ob.mesh];
     const uint4 ti = __ldg(&S.tri_idx[me.tri_off + hr.prim]);

@@ -40,7 +40,7 @@ struct Tracer {
     __device__ int get_medium(const DMaterial &m, float3 w, float3 n) { return dot(w, n) < 0.f ? m.medium_interior : m.medium_exterior; }
 
     /* Scene::IntersectTr (Scene.cpp:45-81); maxT < 0 selects the unbounded form. */
-    __device__ bool intersect_tr(float3 o, float3 d, RayHit &h, int med, Spec<NS> *Tr, float maxT) {
+    __device__ __noinline__ bool intersect_tr(float3 o, float3 d, RayHit &h, int med, Spec<NS> *Tr, float maxT) {
         float tFar = 0.f;
         for (int guard = 0; guard < 256; ++guard) {
             if (!intersect(o, d, h)) return false;
@@ -84,7 +84,7 @@ struct Tracer {
     }
 
     /* ---------------------------------------------------------------- emission programs */
-    __device__ Spec<NS> emission(const DLight &L, const Event &ev, const RayHit &h, bool illum) {
+    __device__ __noinline__ Spec<NS> emission(const DLight &L, const Event &ev, const RayHit &h, bool illum) {
         float4 R[LGPU_MAX_REGS];
         ShadeCtx c;
         c.point = h.point; c.normalS = h.nS; c.uv = h.uv; c.woLy = ev.woL.y; c.eta = ev.eta;
@@ -126,7 +126,7 @@ struct Tracer {
         *pdf = S.fpool[cdf_off + n + 1 + off] / integral;
         return ((float)off + du) / (float)n;
     }
-    __device__ Spec<NS> env_sample_li(Event &ev, const RayHit &h, float &pdf) {   /* EnvironmentLight.cpp:24-45 */
+    __device__ __noinline__ Spec<NS> env_sample_li(Event &ev, const RayHit &h, float &pdf) {   /* EnvironmentLight.cpp:24-45 */
         const DEnv &E = S.env;
         const float u0 = rng.next(), u1 = rng.next();
         float pm, pc; int row;
@@ -149,7 +149,7 @@ struct Tracer {
         pdf = 0.f;
         return Spec<NS>(0.f);
     }
-    __device__ float env_pdf_li(const Event &ev) {   /* EnvironmentLight.cpp:60-67 + Piecewise2D::PDF */
+    __device__ __noinline__ float env_pdf_li(const Event &ev) {   /* EnvironmentLight.cpp:60-67 + Piecewise2D::PDF */
         const DEnv &E = S.env;
         const float theta = spherical_theta(ev.wi) - E.offy;
         const float phi = spherical_phi(ev.wi) - E.offx;
@@ -193,7 +193,7 @@ struct Tracer {
     }
 
     /* Light::Sample_Li for every light kind. */
-    __device__ Spec<NS> sample_li(LRef r, Event &ev, RayHit &h, float &pdf) {
+    __device__ __noinline__ Spec<NS> sample_li(LRef r, Event &ev, RayHit &h, float &pdf) {
         if (r.light < 0) { pdf = 0.f; return Spec<NS>(0.f); }   /* no light to sample */
         const DLight &L = S.lights[r.light];
         if (L.type == LT_ENV) return env_sample_li(ev, h, pdf);
@@ -247,7 +247,7 @@ struct Tracer {
         return (d * d) * (d * d);
     }
     /* Light::PDF_Li(event) at the new hit (MeshLight.cpp:44-53, :158-165, EnvironmentLight.cpp:60-67). */
-    __device__ float pdf_li(LRef r, const Event &ev, const RayHit &h) {
+    __device__ __noinline__ float pdf_li(LRef r, const Event &ev, const RayHit &h) {
         const DLight &L = S.lights[r.light];
         if (L.type == LT_ENV) return env_pdf_li(ev);
         if (L.type != LT_MESH) return 0.f;
@@ -266,7 +266,7 @@ struct Tracer {
         return distSq / (cT * area);
     }
     /* Light::SamplePoint (MeshLight.cpp:55-70, :167-181, PointLight.cpp:40-44). */
-    __device__ Spec<NS> sample_point(LRef r, Event &ev, RayHit &h, float3 &lpoint, float3 &lnormal, float &lpdf) {
+    __device__ __noinline__ Spec<NS> sample_point(LRef r, Event &ev, RayHit &h, float3 &lpoint, float3 &lnormal, float &lpdf) {
         if (r.light < 0) { lpdf = 0.f; lpoint = h.point; return Spec<NS>(0.f); }
         const DLight &L = S.lights[r.light];
         if (L.type == LT_ENV) { lpdf *= 0.f; lpoint = mk(0.f, 0.f, 0.f); return Spec<NS>(0.f); }
@@ -292,7 +292,7 @@ struct Tracer {
         return emission(L, ev, h, true) * L.intensity * INV_PI;
     }
     /* Light::Visibility (MeshLight.cpp:72-81, :183-192, PointLight.cpp:46-55, Spotlight.cpp:69-78, EnvironmentLight.cpp:76-84). */
-    __device__ Spec<NS> visibility(LRef r, float3 p, Event &ev, RayHit &h, float3 lpoint, float3 lnormal, float &lpdf) {
+    __device__ __noinline__ Spec<NS> visibility(LRef r, float3 p, Event &ev, RayHit &h, float3 lpoint, float3 lnormal, float &lpdf) {
         if (r.light < 0) { lpdf = 0.f; return Spec<NS>(0.f); }
         const DLight &L = S.lights[r.light];
         Spec<NS> Tr(1.f);
@@ -321,7 +321,7 @@ struct Tracer {
         return Spec<NS>(0.f);
     }
     /* Light::L at the new hit (MeshLight::L) */
-    __device__ Spec<NS> light_L(LRef r, const Event &ev, const RayHit &h) {
+    __device__ __noinline__ Spec<NS> light_L(LRef r, const Event &ev, const RayHit &h) {
         const DLight &L = S.lights[r.light];
         if (L.type == LT_ENV) return env_le(ev.wi);
         if (L.type == LT_MESH) return emission(L, ev, h, true) * L.intensity * INV_PI;
@@ -358,7 +358,7 @@ struct Tracer {
         return r;
     }
     /* LightSampler::Sample: PowerLightSampler (LightSampler.cpp:17-19) or ManyLightSampler (:17-27, :355-378). */
-    __device__ LRef sample_light(float3 p, float3 nS, float *pdf) {
+    __device__ __noinline__ LRef sample_light(float3 p, float3 nS, float *pdf) {
         if (S.light_strategy == LGPU_LIGHT_STRATEGY_POWER) {
             const float *cdf = S.fpool + S.power_cdf_off;
             const float u = rng.next();
@@ -395,7 +395,7 @@ struct Tracer {
         return r;
     }
     /* LightSampler::Pdf (LightSampler.cpp:21-23, ManyLightSampler.cpp:29-35 + RecursivePDF :380-393, B7, B8). */
-    __device__ float light_pdf(float3 p, float3 nS, int prim, LRef l) {
+    __device__ __noinline__ float light_pdf(float3 p, float3 nS, int prim, LRef l) {
         const DLight &L = S.lights[l.light];
         if (S.light_strategy == LGPU_LIGHT_STRATEGY_POWER) return L.power * S.inv_total_power;
         if (L.type == LT_ENV) return S.inf_power / (S.inf_power + S.tree_power);
@@ -432,7 +432,7 @@ struct Tracer {
     }
 
     /* ---------------------------------------------------------------- BSDF setup */
-    __device__ void setup_bsdf(Bsdf<NS> &b, const DMaterial &m, const Event &ev, const RayHit &h) {
+    __device__ __noinline__ void setup_bsdf(Bsdf<NS> &b, const DMaterial &m, const Event &ev, const RayHit &h) {
         b.m = &m;
         float4 R[LGPU_MAX_REGS];
         ShadeCtx c;
@@ -450,7 +450,7 @@ struct Tracer {
     HD static float power_heuristic(float f, float g) { return (f * f) / (f * f + g * g); }
 
     /* LdMediumPoint (MISVolumetricPathIntegrator.cpp:23-69) */
-    __device__ Spec<NS> ld_medium_point(Event &ev, RayHit &hit, float3 p, LRef lsLight, float3 lsPoint, float3 lsNormal,
+    __device__ __noinline__ Spec<NS> ld_medium_point(Event &ev, RayHit &hit, float3 p, LRef lsLight, float3 lsPoint, float3 lsNormal,
                                         Spec<NS> lsLe, float &lsPdf, float3 &wiOut, float3 sp, float3 sn) {
         /* lsPdf is the PartialLightSample's pdf: Visibility completes it in place, so the second
          * call (equiangular point) starts from the value the first call left. */
