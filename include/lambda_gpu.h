@@ -247,7 +247,16 @@ typedef struct lgpu_render_opts {
     uint32_t seed;            /* counter-based RNG key */
     uint32_t sample_offset;   /* first sample index: resume = same seed, offset = samples done */
     int32_t block_size;       /* 0 = autotuned default */
+    int32_t kernel_mode;      /* lgpu_kernel_mode */
+    int32_t pool_slots;       /* wavefront path-slot pool size, 0 = default (4 Mi slots) */
 } lgpu_render_opts;
+
+/* Execution scheme of one render.  Both produce the same paths (same random-number order). */
+typedef enum lgpu_kernel_mode {
+    LGPU_KERNEL_AUTO = 0,        /* wavefront */
+    LGPU_KERNEL_MEGAKERNEL = 1,  /* one thread runs a whole path */
+    LGPU_KERNEL_WAVEFRONT = 2    /* path state machine + separate traversal kernels */
+} lgpu_kernel_mode;
 
 /* Per-render statistics.  Traversal counters are filled only by lgpu_render_count. */
 typedef struct lgpu_stats {

@@ -78,7 +78,10 @@ class RenderOpts(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
                 ("max_bounces", C.c_int32), ("min_bounces", C.c_int32), ("integrator", C.c_int32),
                 ("spectral_mode", C.c_int32), ("seed", C.c_uint32), ("sample_offset", C.c_uint32),
-                ("block_size", C.c_int32)]
+                ("block_size", C.c_int32), ("kernel_mode", C.c_int32), ("pool_slots", C.c_int32)]
+
+
+KERNEL_AUTO, KERNEL_MEGAKERNEL, KERNEL_WAVEFRONT = 0, 1, 2
 
 
 class Stats(C.Structure):
@@ -89,6 +92,6 @@ class Stats(C.Structure):
 
 
 def render_opts(width, height, spp, max_bounces, min_bounces=3, seed=1, spectral=SPECTRAL_RGB3,
-                sample_offset=0, integrator=INTEGRATOR_GPU_MISVOLPATH, block_size=0):
+                sample_offset=0, integrator=INTEGRATOR_GPU_MISVOLPATH, block_size=0, kernel_mode=0, pool_slots=0):
     return RenderOpts(width, height, spp, max_bounces, min_bounces, integrator, spectral, seed,
-                      sample_offset, block_size)
+                      sample_offset, block_size, kernel_mode, pool_slots)

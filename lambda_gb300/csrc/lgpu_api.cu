@@ -26,6 +26,7 @@
 #include "lgpu_device.cuh"
 #include "lgpu_launch.h"
 #include "lgpu_lighttree.h"
+#include "lgpu_wavefront.cuh"
 
 using namespace lg;
 
@@ -44,6 +45,17 @@ struct lgpu_context {
     uint64_t *d_ids = nullptr;
     size_t ids_cap = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    /* wavefront pool */
+    void *w_states = nullptr;
+    size_t w_state_bytes = 0;
+    size_t w_slots = 0;
+    float4 *w_qo = nullptr, *w_qd = nullptr, *w_res = nullptr;
+    int *w_resobj = nullptr, *w_qa = nullptr, *w_qb = nullptr, *w_counts = nullptr;
+    unsigned long long *w_next = nullptr;
+    int *h_count = nullptr;   /* pinned */
+    float4 *w_paths = nullptr;
+    size_t w_paths_cap = 0;
+    int last_iterations = 0;
 };
 
 namespace {
@@ -282,6 +294,9 @@ LGPU_API void lgpu_destroy(lgpu_context *c) {
     cudaFree(c->d_ids);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    cudaFree(c->w_states); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
+    cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_counts); cudaFree(c->w_next); cudaFree(c->w_paths);
+    if (c->h_count) cudaFreeHost(c->h_count);
     delete c;
 }
 
@@ -814,8 +829,138 @@ int check_opts(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_o
     return LGPU_OK;
 }
 
+/* Grow the wavefront pool to `slots` path slots of `state_bytes` each. */
+int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes) {
+    if (c->w_slots >= slots && c->w_state_bytes == state_bytes) return LGPU_OK;
+    cudaFree(c->w_states); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
+    cudaFree(c->w_qa); cudaFree(c->w_qb);
+    c->w_states = nullptr; c->w_qo = c->w_qd = c->w_res = nullptr; c->w_resobj = c->w_qa = c->w_qb = nullptr;
+    c->w_slots = 0;
+    cudaError_t e = cudaMalloc(&c->w_states, slots * state_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_qo, slots * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_qd, slots * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_res, slots * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_resobj, slots * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_qa, slots * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_qb, slots * sizeof(int));
+    if (e == cudaSuccess && !c->w_counts) e = cudaMalloc(&c->w_counts, 2 * sizeof(int));
+    if (e == cudaSuccess && !c->w_next) e = cudaMalloc(&c->w_next, sizeof(unsigned long long));
+    if (e == cudaSuccess && !c->h_count) e = cudaMallocHost(&c->h_count, 2 * sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(c, e, "wavefront pool allocation");
+    c->w_slots = slots;
+    c->w_state_bytes = state_bytes;
+    return LGPU_OK;
+}
+
+/* Run the wavefront over `n` paths (chunk indices 0..n-1 = path ids base.. or ids[]), writing
+ * radiance per path into paths_out. */
+int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o, const uint64_t *ids,
+                  uint64_t base, uint64_t n, float4 *paths_out, bool count, cudaStream_t st) {
+    const bool hero = o->spectral_mode == LGPU_SPECTRAL_HERO4;
+    const size_t sb = hero ? wave_state_bytes_4_0() : wave_state_bytes_3_0();
+    const size_t want = o->pool_slots > 0 ? (size_t)o->pool_slots : ((size_t)4 << 20);
+    const size_t slots = (size_t)std::min<uint64_t>(n, want);
+    if (slots == 0) return LGPU_OK;
+    int rc = ensure_pool(c, slots, sb);
+    if (rc) return rc;
+    WaveArgs W;
+    std::memset(&W, 0, sizeof(W));
+    W.S = c->S;
+    W.cam = make_cam(cam, o);
+    W.rp.spp = o->spp; W.rp.max_bounces = o->max_bounces; W.rp.min_bounces = o->min_bounces;
+    W.rp.seed = o->seed; W.rp.sample_offset = o->sample_offset;
+    W.states = c->w_states;
+    W.qo = c->w_qo; W.qd = c->w_qd; W.res = c->w_res; W.res_obj = c->w_resobj;
+    W.next_path = c->w_next;
+    W.n_paths = n;
+    W.base = base;
+    W.ids = ids;
+    W.path_out = paths_out;
+    W.counters = c->d_counters;
+    auto resume = [&](int m, int start_new) {
+        if (hero) return count ? wave_resume_4_1(W, m, start_new, st) : wave_resume_4_0(W, m, start_new, st);
+        return count ? wave_resume_3_1(W, m, start_new, st) : wave_resume_3_0(W, m, start_new, st);
+    };
+    int *qa = c->w_qa, *qb = c->w_qb, *ca = c->w_counts, *cb = c->w_counts + 1;
+    const unsigned long long nextInit = slots;
+    cudaMemcpyAsync(c->w_next, &nextInit, sizeof(nextInit), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(ca, 0, sizeof(int), st);
+    W.queue_in = nullptr; W.queue_out = qa; W.count_out = ca;
+    cudaError_t e = resume((int)slots, 1);
+    if (e != cudaSuccess) return cuda_fail(c, e, "wavefront start");
+    int iters = 0;
+    for (;;) {
+        cudaMemcpyAsync(c->h_count, ca, sizeof(int), cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "wavefront");
+        const int m = *c->h_count;
+        if (m <= 0) break;
+        if (++iters > 100000) return fail(c, LGPU_ERR_TIMEOUT, "wavefront did not drain");
+        cudaMemsetAsync(cb, 0, sizeof(int), st);
+        W.queue_in = qa; W.queue_out = qb; W.count_out = cb;
+        e = count ? wave_trace_3_1(W, m, st) : wave_trace_3_0(W, m, st);
+        if (e == cudaSuccess) e = resume(m, 0);
+        if (e != cudaSuccess) return cuda_fail(c, e, "wavefront iteration");
+        std::swap(qa, qb);
+        std::swap(ca, cb);
+    }
+    c->last_iterations = iters;
+    return LGPU_OK;
+}
+
+bool use_wavefront(const lgpu_render_opts *o) { return o->kernel_mode != LGPU_KERNEL_MEGAKERNEL; }
+
+int ensure_paths(lgpu_context *c, size_t n) {
+    if (c->w_paths_cap >= n) return LGPU_OK;
+    cudaFree(c->w_paths);
+    c->w_paths = nullptr;
+    c->w_paths_cap = 0;
+    cudaError_t e = cudaMalloc(&c->w_paths, n * sizeof(float4));
+    if (e != cudaSuccess) return cuda_fail(c, e, "per-path buffer");
+    c->w_paths_cap = n;
+    return LGPU_OK;
+}
+
+/* Whole-frame wavefront render into a device film (chunks of whole pixels). */
+int wavefront_frame(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o, float4 *film,
+                    float4 *paths_all, bool count, cudaStream_t st) {
+    const uint64_t px = (uint64_t)o->width * o->height;
+    const uint64_t spp = (uint64_t)o->spp;
+    const uint64_t max_chunk = (uint64_t)1 << 28;   /* 256 Mi paths = 4 GiB of per-path radiance */
+    uint64_t chunk_px = std::max<uint64_t>(1, std::min<uint64_t>(px, max_chunk / spp));
+    for (uint64_t p0 = 0; p0 < px; p0 += chunk_px) {
+        const uint64_t npx = std::min(chunk_px, px - p0);
+        const uint64_t n = npx * spp;
+        float4 *out;
+        if (paths_all) out = paths_all + p0 * spp;
+        else {
+            int rc = ensure_paths(c, n);
+            if (rc) return rc;
+            out = c->w_paths;
+        }
+        int rc = run_wavefront(c, cam, o, nullptr, p0 * spp, n, out, count, st);
+        if (rc) return rc;
+        if (film) {
+            cudaError_t e = film_reduce(out, film, p0, npx, o->spp, st);
+            if (e != cudaSuccess) return cuda_fail(c, e, "film reduce");
+        }
+    }
+    return LGPU_OK;
+}
+
 int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o, float4 *film, float4 *paths,
                 const uint64_t *ids, uint64_t n, bool count, cudaStream_t s) {
+    if (use_wavefront(o)) {
+        if (count) cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
+        cudaEventRecord(c->ev0, s);
+        int rc;
+        if (ids) rc = run_wavefront(c, cam, o, ids, 0, n, paths, count, s);
+        else rc = wavefront_frame(c, cam, o, film, paths, count, s);
+        if (rc) return rc;
+        cudaEventRecord(c->ev1, s);
+        c->stats.paths = n;
+        return LGPU_OK;
+    }
     LaunchArgs a;
     a.S = c->S;
     a.cam = make_cam(cam, o);

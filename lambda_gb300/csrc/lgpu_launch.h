@@ -37,6 +37,18 @@ inline cudaError_t launch_render(const LaunchArgs &a) {
     if (a.hero) return a.count ? launch_render_4_1(a) : launch_render_4_0(a);
     return a.count ? launch_render_3_1(a) : launch_render_3_0(a);
 }
+struct WaveArgs;
+cudaError_t wave_resume_3_0(const WaveArgs &W, int n, int start_new, cudaStream_t st);
+cudaError_t wave_resume_3_1(const WaveArgs &W, int n, int start_new, cudaStream_t st);
+cudaError_t wave_resume_4_0(const WaveArgs &W, int n, int start_new, cudaStream_t st);
+cudaError_t wave_resume_4_1(const WaveArgs &W, int n, int start_new, cudaStream_t st);
+cudaError_t wave_trace_3_0(const WaveArgs &W, int n, cudaStream_t st);
+cudaError_t wave_trace_3_1(const WaveArgs &W, int n, cudaStream_t st);
+size_t wave_state_bytes_3_0();
+size_t wave_state_bytes_4_0();
+size_t wave_state_bytes_3_1();
+size_t wave_state_bytes_4_1();
+cudaError_t film_reduce(const float4 *paths, float4 *film, uint64_t first_px, uint64_t n_px, int spp, cudaStream_t st);
 cudaError_t launch_intersect(const DeviceScene &S, const float *rays, uint32_t *hits, float *uvs, uint64_t n, cudaStream_t s);
 
 }  // namespace lg

@@ -11,6 +11,7 @@
 
 #include "lgpu_integrator.cuh"
 #include "lgpu_launch.h"
+#include "lgpu_wavefront.cuh"
 
 #ifndef LGPU_NS
 #define LGPU_NS 3
@@ -147,7 +148,98 @@ cudaError_t LG_CAT(launch_render_, LGPU_NS, LGPU_COUNT)(const LaunchArgs &a) {
     return cudaGetLastError();
 }
 
+/* ---------------------------------------------------------------- wavefront kernels */
+template <int NS, bool COUNT>
+__global__ void __launch_bounds__(128) k_wave_resume(WaveArgs W, int n, int start_new) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int slot = start_new ? i : W.queue_in[i];
+    PState<NS> &s = reinterpret_cast<PState<NS> *>(W.states)[slot];
+    Wave<NS, COUNT> w{W, s, slot};
+    if (start_new) {
+        w.start_path((uint64_t)i);
+    } else {
+        w.rng.key = s.key;
+        w.rng.dim = s.dim;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) w.lam.l[k] = s.lam[k];
+    }
+    for (int guard = 0; guard < 1 << 20; ++guard) {
+        w.run();
+        if (s.pc != PC_DONE) break;   /* a query is pending */
+        w.finish();
+        const uint64_t nxt = grab_path(W);
+        if (nxt >= W.n_paths) return;
+        w.start_path(nxt);
+    }
+    s.key = w.rng.key;
+    s.dim = w.rng.dim;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s.lam[k] = w.lam.l[k];
+}
+
+cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, int start_new, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_wave_resume<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, 0, st>>>(W, n, start_new);
+    return cudaGetLastError();
+}
+size_t LG_CAT(wave_state_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PState<LGPU_NS>); }
+
+#if LGPU_NS == 3
+/* Answer every queued query: closest hit (Scene::Intersect) or occlusion (rtcOccluded1). */
+template <bool COUNT>
+__global__ void __launch_bounds__(256) k_wave_trace(WaveArgs W, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    TravStats st = {0u, 0u, 0u};
+    if (i < n) {
+        const int slot = W.queue_in[i];
+        const float4 o = W.qo[slot], d = W.qd[slot];
+        HitRec hr;
+        if (__float_as_int(d.w) == Q_CLOSEST) {
+            const bool ok = traverse<COUNT>(W.S, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), finf(), false, &hr, &st);
+            W.res[slot] = ok ? make_float4(hr.t, hr.u, hr.v, __int_as_float(hr.prim)) : make_float4(finf(), 0.f, 0.f, 0.f);
+            W.res_obj[slot] = ok ? hr.obj : -1;
+        } else {
+            const bool occ = traverse<COUNT>(W.S, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), o.w, true, &hr, &st);
+            W.res[slot] = make_float4(occ ? 1.f : 0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    if (COUNT) {
+        const unsigned long long a = __reduce_add_sync(0xffffffffu, st.nodes);
+        const unsigned long long b = __reduce_add_sync(0xffffffffu, st.tris);
+        const unsigned long long c = __reduce_add_sync(0xffffffffu, st.rays);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&W.counters[0], a);
+            atomicAdd(&W.counters[1], b);
+            atomicAdd(&W.counters[2], c);
+        }
+    }
+}
+cudaError_t LG_CAT(wave_trace_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_wave_trace<LGPU_COUNT != 0><<<(n + 255) / 256, 256, 0, st>>>(W, n);
+    return cudaGetLastError();
+}
+#endif
+
 #if LGPU_NS == 3 && LGPU_COUNT == 0
+/* film[pixel] += (sum of the pixel's spp path radiances, spp): Film::AddSample for a whole tile. */
+__global__ void k_film_reduce(const float4 *paths, float4 *film, uint64_t first_px, uint64_t n_px, int spp) {
+    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_px) return;
+    float r = 0.f, g = 0.f, b = 0.f;
+    const float4 *q = paths + p * (uint64_t)spp;
+    for (int s = 0; s < spp; ++s) { const float4 v = q[s]; r += v.x; g += v.y; b += v.z; }
+    float4 f = film[first_px + p];
+    f.x += r; f.y += g; f.z += b; f.w += (float)spp;
+    film[first_px + p] = f;
+}
+cudaError_t film_reduce(const float4 *paths, float4 *film, uint64_t first_px, uint64_t n_px, int spp, cudaStream_t st) {
+    if (n_px == 0) return cudaSuccess;
+    k_film_reduce<<<(unsigned)((n_px + 255) / 256), 256, 0, st>>>(paths, film, first_px, n_px, spp);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_intersect(const DeviceScene &S, const float *rays, uint32_t *hits, float *uvs, uint64_t n, cudaStream_t s) {
     const int bs = 128;
     const uint64_t blocks = (n + bs - 1) / bs;

@@ -14,6 +14,8 @@ from tests.parity import path_agreement, sample_ids
 
 pytestmark = pytest.mark.gpu
 
+MODES = pytest.mark.parametrize("mode", [1, 2], ids=["megakernel", "wavefront"])
+
 
 def _render_both(lg, sb, cam, opts, n):
     ids = sample_ids(opts, n)
@@ -24,44 +26,54 @@ def _render_both(lg, sb, cam, opts, n):
     return g, o
 
 
-def test_cornell_rgb_paths(gpu_lib):
+@MODES
+def test_cornell_rgb_paths(gpu_lib, mode):
     from lambda_gb300 import configs
     sb, cam, opts = configs.cornell(48, 48, 4)
+    opts.kernel_mode = mode
     g, o = _render_both(gpu_lib, sb, cam, opts, 48 * 48 * 4)
     frac, ok = path_agreement(g, o)
     assert np.isfinite(g).all()
     assert frac >= 0.99, "per-path agreement %.5f" % frac
 
 
-def test_cornell_hero_paths(gpu_lib):
+@MODES
+def test_cornell_hero_paths(gpu_lib, mode):
     from lambda_gb300 import abi, configs
     sb, cam, opts = configs.cornell(32, 32, 4)
+    opts.kernel_mode = mode
     opts.spectral_mode = abi.SPECTRAL_HERO4
     g, o = _render_both(gpu_lib, sb, cam, opts, 32 * 32 * 4)
     frac, _ = path_agreement(g, o)
     assert frac >= 0.99, "per-path agreement %.5f" % frac
 
 
-def test_terrain_small_paths(gpu_lib):
+@MODES
+def test_terrain_small_paths(gpu_lib, mode):
     from lambda_gb300 import configs
     sb, cam, opts = configs.terrain(64, 36, 4, grid=96, n_emitters=300)
+    opts.kernel_mode = mode
     g, o = _render_both(gpu_lib, sb, cam, opts, 64 * 36 * 4)
     frac, _ = path_agreement(g, o)
     assert frac >= 0.99, "per-path agreement %.5f" % frac
 
 
-def test_volume_small_paths(gpu_lib):
+@MODES
+def test_volume_small_paths(gpu_lib, mode):
     from lambda_gb300 import configs
     sb, cam, opts = configs.volume(48, 27, 4, max_depth=12, n_instances=40, sphere_res=(24, 24))
+    opts.kernel_mode = mode
     g, o = _render_both(gpu_lib, sb, cam, opts, 48 * 27 * 4)
     frac, _ = path_agreement(g, o)
     assert frac >= 0.99, "per-path agreement %.5f" % frac
 
 
-def test_film_matches_paths(gpu_lib):
+@MODES
+def test_film_matches_paths(gpu_lib, mode):
     """lgpu_render's film equals the per-pixel sum of the per-path radiance."""
     from lambda_gb300 import configs
     sb, cam, opts = configs.cornell(32, 32, 32)
+    opts.kernel_mode = mode
     r = gpu_lib.Renderer(sb)
     film = r.render(cam, opts)
     ids = np.arange(32 * 32 * 32, dtype=np.uint64)
@@ -69,3 +81,20 @@ def test_film_matches_paths(gpu_lib):
     r.close()
     np.testing.assert_allclose(film[..., 3], 32.0)
     np.testing.assert_allclose(film[..., :3], p[..., :3].sum(axis=2), rtol=1e-4, atol=1e-5)
+
+
+def test_wavefront_equals_megakernel_terrain(gpu_lib):
+    """The two execution schemes draw the same random numbers in the same order: same paths."""
+    from lambda_gb300 import configs
+    sb, cam, opts = configs.terrain(64, 36, 8, grid=96, n_emitters=300)
+    ids = np.arange(64 * 36 * 8, dtype=np.uint64)
+    r = gpu_lib.Renderer(sb)
+    opts.kernel_mode = 1
+    a = r.render_paths(cam, opts, ids)
+    opts.kernel_mode = 2
+    opts.pool_slots = 1000   # small pool: exercises path regeneration
+    b = r.render_paths(cam, opts, ids)
+    r.close()
+    np.testing.assert_array_equal(a[:, 3], b[:, 3])
+    frac, _ = path_agreement(a, b, rel=1e-5)
+    assert frac >= 0.999
