@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--spp", type=int, default=64)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--mode", default="auto", choices=["auto", "megakernel", "wavefront"])
+    p.add_argument("--pool", type=int, default=0, help="wavefront path-slot pool size (0 = default)")
     return p.parse_args()
 
 
@@ -182,6 +184,8 @@ def main():
     torch.cuda.set_device(dev)
     sb, cam, opts = configs.terrain(args.width, args.height, args.spp, 6)
     opts.seed = 1 + rank
+    opts.kernel_mode = {"auto": abi.KERNEL_AUTO, "megakernel": abi.KERNEL_MEGAKERNEL, "wavefront": abi.KERNEL_WAVEFRONT}[args.mode]
+    opts.pool_slots = args.pool
     r = lg.Renderer(sb, device=dev)
     W, H, spp = opts.width, opts.height, opts.spp
     paths = W * H * spp

@@ -50,7 +50,7 @@ struct lgpu_context {
     size_t w_state_bytes = 0;
     size_t w_slots = 0;
     float4 *w_qo = nullptr, *w_qd = nullptr, *w_res = nullptr;
-    int *w_resobj = nullptr, *w_qa = nullptr, *w_qb = nullptr, *w_counts = nullptr;
+    int *w_resobj = nullptr, *w_qa = nullptr, *w_qb = nullptr, *w_counts = nullptr, *w_free = nullptr;
     unsigned long long *w_next = nullptr;
     int *h_count = nullptr;   /* pinned */
     float4 *w_paths = nullptr;
@@ -295,7 +295,7 @@ LGPU_API void lgpu_destroy(lgpu_context *c) {
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     cudaFree(c->w_states); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
-    cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_counts); cudaFree(c->w_next); cudaFree(c->w_paths);
+    cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_counts); cudaFree(c->w_next); cudaFree(c->w_paths); cudaFree(c->w_free);
     if (c->h_count) cudaFreeHost(c->h_count);
     delete c;
 }
@@ -833,19 +833,20 @@ int check_opts(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_o
 int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes) {
     if (c->w_slots >= slots && c->w_state_bytes == state_bytes) return LGPU_OK;
     cudaFree(c->w_states); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
-    cudaFree(c->w_qa); cudaFree(c->w_qb);
-    c->w_states = nullptr; c->w_qo = c->w_qd = c->w_res = nullptr; c->w_resobj = c->w_qa = c->w_qb = nullptr;
+    cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_free);
+    c->w_states = nullptr; c->w_qo = c->w_qd = c->w_res = nullptr; c->w_resobj = c->w_qa = c->w_qb = c->w_free = nullptr;
     c->w_slots = 0;
     cudaError_t e = cudaMalloc(&c->w_states, slots * state_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->w_qo, slots * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_qd, slots * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_res, slots * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_resobj, slots * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&c->w_qa, slots * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&c->w_qb, slots * sizeof(int));
-    if (e == cudaSuccess && !c->w_counts) e = cudaMalloc(&c->w_counts, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_qa, LG_NSEG * slots * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_qb, LG_NSEG * slots * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_free, slots * sizeof(int));
+    if (e == cudaSuccess && !c->w_counts) e = cudaMalloc(&c->w_counts, (2 * LG_NSEG + 2) * sizeof(int));
     if (e == cudaSuccess && !c->w_next) e = cudaMalloc(&c->w_next, sizeof(unsigned long long));
-    if (e == cudaSuccess && !c->h_count) e = cudaMallocHost(&c->h_count, 2 * sizeof(int));
+    if (e == cudaSuccess && !c->h_count) e = cudaMallocHost(&c->h_count, (2 * LG_NSEG + 2) * sizeof(int));
     if (e != cudaSuccess) return cuda_fail(c, e, "wavefront pool allocation");
     c->w_slots = slots;
     c->w_state_bytes = state_bytes;
@@ -853,7 +854,8 @@ int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes) {
 }
 
 /* Run the wavefront over `n` paths (chunk indices 0..n-1 = path ids base.. or ids[]), writing
- * radiance per path into paths_out. */
+ * radiance per path into paths_out.  Per iteration: one count read-back, then trace, resume,
+ * spawn (new paths into freed slots) and advance. */
 int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o, const uint64_t *ids,
                   uint64_t base, uint64_t n, float4 *paths_out, bool count, cudaStream_t st) {
     const bool hero = o->spectral_mode == LGPU_SPECTRAL_HERO4;
@@ -877,29 +879,37 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     W.ids = ids;
     W.path_out = paths_out;
     W.counters = c->d_counters;
-    auto resume = [&](int m, int start_new) {
-        if (hero) return count ? wave_resume_4_1(W, m, start_new, st) : wave_resume_4_0(W, m, start_new, st);
-        return count ? wave_resume_3_1(W, m, start_new, st) : wave_resume_3_0(W, m, start_new, st);
+    W.cap = (int)slots;
+    W.free_list = c->w_free;
+    auto resume = [&](int m, int mode) {
+        if (hero) return count ? wave_resume_4_1(W, m, mode, st) : wave_resume_4_0(W, m, mode, st);
+        return count ? wave_resume_3_1(W, m, mode, st) : wave_resume_3_0(W, m, mode, st);
     };
-    int *qa = c->w_qa, *qb = c->w_qb, *ca = c->w_counts, *cb = c->w_counts + 1;
-    const unsigned long long nextInit = slots;
-    cudaMemcpyAsync(c->w_next, &nextInit, sizeof(nextInit), cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(ca, 0, sizeof(int), st);
+    int *qa = c->w_qa, *qb = c->w_qb;
+    int *ca = c->w_counts, *cb = c->w_counts + LG_NSEG;
+    W.free_count = c->w_counts + 2 * LG_NSEG;
+    const unsigned long long zero = 0;
+    cudaMemcpyAsync(c->w_next, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(c->w_counts, 0, (2 * LG_NSEG + 2) * sizeof(int), st);
+    /* first spawn fills the whole pool */
     W.queue_in = nullptr; W.queue_out = qa; W.count_out = ca;
-    cudaError_t e = resume((int)slots, 1);
+    cudaError_t e = resume((int)slots, 2);
     if (e != cudaSuccess) return cuda_fail(c, e, "wavefront start");
     int iters = 0;
     for (;;) {
-        cudaMemcpyAsync(c->h_count, ca, sizeof(int), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(c->h_count, ca, LG_NSEG * sizeof(int), cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(c, e, "wavefront");
-        const int m = *c->h_count;
+        int m = 0;
+        W.seg_off[0] = 0;
+        for (int k = 0; k < LG_NSEG; ++k) { m += c->h_count[k]; W.seg_off[k + 1] = m; }
         if (m <= 0) break;
         if (++iters > 100000) return fail(c, LGPU_ERR_TIMEOUT, "wavefront did not drain");
-        cudaMemsetAsync(cb, 0, sizeof(int), st);
+        cudaMemsetAsync(cb, 0, LG_NSEG * sizeof(int), st);
         W.queue_in = qa; W.queue_out = qb; W.count_out = cb;
         e = count ? wave_trace_3_1(W, m, st) : wave_trace_3_0(W, m, st);
         if (e == cudaSuccess) e = resume(m, 0);
+        if (e == cudaSuccess) e = resume(m, 1);   /* spawn into the slots freed by this resume */
         if (e != cudaSuccess) return cuda_fail(c, e, "wavefront iteration");
         std::swap(qa, qb);
         std::swap(ca, cb);

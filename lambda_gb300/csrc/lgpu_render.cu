@@ -150,37 +150,71 @@ cudaError_t LG_CAT(launch_render_, LGPU_NS, LGPU_COUNT)(const LaunchArgs &a) {
 
 /* ---------------------------------------------------------------- wavefront kernels */
 template <int NS, bool COUNT>
-__global__ void __launch_bounds__(128) k_wave_resume(WaveArgs W, int n, int start_new) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int slot = start_new ? i : W.queue_in[i];
-    PState<NS> &s = reinterpret_cast<PState<NS> *>(W.states)[slot];
-    Wave<NS, COUNT> w{W, s, slot};
-    if (start_new) {
-        w.start_path((uint64_t)i);
-    } else {
-        w.rng.key = s.key;
-        w.rng.dim = s.dim;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) w.lam.l[k] = s.lam[k];
-    }
-    for (int guard = 0; guard < 1 << 20; ++guard) {
-        w.run();
-        if (s.pc != PC_DONE) break;   /* a query is pending */
-        w.finish();
-        const uint64_t nxt = grab_path(W);
-        if (nxt >= W.n_paths) return;
-        w.start_path(nxt);
-    }
+__device__ __forceinline__ void wave_save(Wave<NS, COUNT> &w, PState<NS> &s) {
     s.key = w.rng.key;
     s.dim = w.rng.dim;
 #pragma unroll
     for (int k = 0; k < 4; ++k) s.lam[k] = w.lam.l[k];
 }
 
+/* Continue every slot of the (segmented) input queue until its next query or its end. */
+template <int NS, bool COUNT>
+__global__ void __launch_bounds__(128) k_wave_resume(WaveArgs W, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int seg = 0;
+#pragma unroll
+    for (int k = 1; k < LG_NSEG; ++k) seg += (i >= W.seg_off[k]) ? 1 : 0;
+    const int slot = W.queue_in[seg * W.cap + (i - W.seg_off[seg])];
+    PState<NS> &s = reinterpret_cast<PState<NS> *>(W.states)[slot];
+    Wave<NS, COUNT> w{W, s, slot};
+    w.rng.key = s.key;
+    w.rng.dim = s.dim;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) w.lam.l[k] = s.lam[k];
+    w.run();
+    if (s.pc == PC_DONE) { w.finish(); push_free(W, slot); return; }
+    wave_save(w, s);
+}
+
+/* Start new paths in free slots: consecutive path ids go to consecutive free-list entries, so the
+ * warps of a spawn trace neighbouring samples of one pixel.  Slots come from the free list, or from
+ * the untouched tail of the pool on the first spawn (free_list == nullptr). */
+template <int NS, bool COUNT>
+__global__ void __launch_bounds__(128) k_wave_spawn(WaveArgs W, int n_max, int fresh) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nfree = fresh ? n_max : *W.free_count;
+    const unsigned long long next = *W.next_path;
+    const unsigned long long left = next < W.n_paths ? W.n_paths - next : 0ull;
+    const int m = (int)(nfree < (int)min(left, (unsigned long long)0x7fffffff) ? nfree : (int)left);
+    if (i >= m) return;
+    const int slot = fresh ? i : W.free_list[i];
+    PState<NS> &s = reinterpret_cast<PState<NS> *>(W.states)[slot];
+    Wave<NS, COUNT> w{W, s, slot};
+    w.start_path(next + (uint64_t)i);
+    w.run();
+    if (s.pc == PC_DONE) { w.finish(); return; }   /* slot idles until the next spawn reuses it */
+    wave_save(w, s);
+}
+/* next_path += paths started by the last spawn; clear the free list. */
+static __global__ void k_wave_advance(WaveArgs W, int n_max, int fresh) {
+    const int nfree = fresh ? n_max : *W.free_count;
+    const unsigned long long next = *W.next_path;
+    const unsigned long long left = next < W.n_paths ? W.n_paths - next : 0ull;
+    const unsigned long long m = (unsigned long long)nfree < left ? (unsigned long long)nfree : left;
+    *W.next_path = next + m;
+    *W.free_count = 0;
+}
+
 cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, int start_new, cudaStream_t st) {
+    if (start_new) {
+        /* spawn into up to n slots (fresh pool or free list), then advance the path counter */
+        if (n > 0) k_wave_spawn<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, 0, st>>>(W, n, start_new == 2);
+        k_wave_advance<<<1, 1, 0, st>>>(W, n, start_new == 2);
+        return cudaGetLastError();
+    }
     if (n <= 0) return cudaSuccess;
-    k_wave_resume<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, 0, st>>>(W, n, start_new);
+    k_wave_resume<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, 0, st>>>(W, n);
     return cudaGetLastError();
 }
 size_t LG_CAT(wave_state_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PState<LGPU_NS>); }
@@ -192,7 +226,10 @@ __global__ void __launch_bounds__(256) k_wave_trace(WaveArgs W, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     TravStats st = {0u, 0u, 0u};
     if (i < n) {
-        const int slot = W.queue_in[i];
+        int seg = 0;
+#pragma unroll
+        for (int k = 1; k < LG_NSEG; ++k) seg += (i >= W.seg_off[k]) ? 1 : 0;
+        const int slot = W.queue_in[seg * W.cap + (i - W.seg_off[seg])];
         const float4 o = W.qo[slot], d = W.qd[slot];
         HitRec hr;
         if (__float_as_int(d.w) == Q_CLOSEST) {

@@ -30,6 +30,21 @@ enum : int {
     PC_VIS_OCCL, PC_VIS_TR, PC_TR_STEP, PC_DONE
 };
 enum : int { VIS_AREA = 0, VIS_POINT = 1, VIS_ESCAPE = 2 };
+
+/* Queue segments: slots waiting on a query are grouped by the program point that resumes them, so a
+ * warp of k_resume mostly runs one branch of the state machine and k_trace sees closest-hit and
+ * occlusion queries in separate runs. */
+#define LG_NSEG 6
+__host__ __device__ __forceinline__ int seg_of(int pc) {
+    switch (pc) {
+    case PC_TOP_HIT: return 0;
+    case PC_SURF_EXT: return 1;
+    case PC_NULL_EXT: return 2;
+    case PC_MED_EXT: return 3;
+    case PC_VIS_OCCL: return 4;
+    default: return 5;   /* PC_TR_STEP */
+    }
+}
 enum : int { TR_TEMP = 0, TR_EVENT = 1 };
 
 template <int NS>
@@ -79,9 +94,13 @@ struct WaveArgs {
     float4 *qo, *qd;              /* per slot: origin + tmax, direction + query type */
     float4 *res;                  /* per slot: t, u, v, prim (closest) or occluded flag */
     int *res_obj;
-    const int *queue_in;
+    const int *queue_in;          /* LG_NSEG segments of `cap` entries */
     int *queue_out;
-    int *count_out;
+    int *count_out;               /* LG_NSEG counters of queue_out */
+    int seg_off[LG_NSEG + 1];     /* prefix offsets of the queue_in segments */
+    int cap;
+    int *free_list;               /* slots whose path ended this iteration */
+    int *free_count;
     unsigned long long *next_path;
     uint64_t n_paths;             /* paths in this chunk */
     uint64_t base;                /* path id of chunk index 0 (when ids == nullptr) */
@@ -90,20 +109,22 @@ struct WaveArgs {
     unsigned long long *counters; /* traversal counters (COUNT variant) */
 };
 
-/* Append `slot` to the next queue; one atomic per coalesced group. */
-__device__ __forceinline__ void push_queue(const WaveArgs &W, int slot) {
+/* Append `slot` to segment `seg` of the next queue; one atomic per group of lanes with the same
+ * segment. */
+__device__ __forceinline__ void push_queue(const WaveArgs &W, int slot, int seg) {
+    cgx::coalesced_group all = cgx::coalesced_threads();
+    cgx::coalesced_group g = cgx::labeled_partition(all, seg);
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(W.count_out + seg, (int)g.size());
+    base = g.shfl(base, 0);
+    W.queue_out[seg * W.cap + base + g.thread_rank()] = slot;
+}
+__device__ __forceinline__ void push_free(const WaveArgs &W, int slot) {
     cgx::coalesced_group g = cgx::coalesced_threads();
     int base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(W.count_out, (int)g.size());
+    if (g.thread_rank() == 0) base = atomicAdd(W.free_count, (int)g.size());
     base = g.shfl(base, 0);
-    W.queue_out[base + g.thread_rank()] = slot;
-}
-__device__ __forceinline__ uint64_t grab_path(const WaveArgs &W) {
-    cgx::coalesced_group g = cgx::coalesced_threads();
-    unsigned long long base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(W.next_path, (unsigned long long)g.size());
-    base = g.shfl(base, 0);
-    return (uint64_t)base + g.thread_rank();
+    W.free_list[base + g.thread_rank()] = slot;
 }
 
 template <int NS, bool COUNT>
@@ -121,7 +142,7 @@ struct Wave {
         W.qo[slot] = make_float4(o.x, o.y, o.z, tmax);
         W.qd[slot] = make_float4(d.x, d.y, d.z, __int_as_float(type));
         s.pc = next;
-        push_queue(W, slot);
+        push_queue(W, slot, seg_of(next));
     }
     /* result of the last closest query: valid hit as Scene::Intersect defines it */
     __device__ bool closest(HitRec &hr) {
