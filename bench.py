@@ -194,6 +194,12 @@ def main():
     stream = torch.cuda.current_stream().cuda_stream
     # counting launch (outside the timed region): nodes / triangles / rays of one frame
     stats = r.render_count(cam, opts)
+    breakdown = None
+    if os.environ.get("LGPU_PROFILE"):
+        r.render_device(cam, opts, film.data_ptr(), stream=stream)
+        torch.cuda.synchronize()
+        b = r.stats()
+        breakdown = {k: b[k] for k in ("trace_ms", "shade_ms", "spawn_ms", "iterations", "pool_slots")}
     for _ in range(args.warmup):
         r.render_device(cam, opts, film.data_ptr(), stream=stream)
     torch.cuda.synchronize()
@@ -232,6 +238,10 @@ def main():
     else:
         e2e_ms = e2e_s * 1e3
     value = paths * args.steps * world / (total_ms / 1e3) / 1e6
+    st_now = r.stats()
+    # kernels of ours per timed step: megakernel 1; wavefront 3 per iteration (trace, resume, spawn)
+    # + 1 advance per iteration + 1 film reduction (+ first spawn)
+    launches = args.steps * (1 if opts.kernel_mode == abi.KERNEL_MEGAKERNEL else (4 * max(1, st_now["iterations"]) + 3))
     e2e = paths * args.steps * world / (e2e_ms / 1e3) / 1e6
     if rank != 0:
         if dist:
@@ -260,7 +270,9 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
             "config": cfg, "parallelism": "replicas" if world > 1 else "single GPU",
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": W * H * 16, "d2h_bytes_per_step": W * H * 16},
-            "gpu_launches": args.steps, "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
+    if breakdown:
+        line["wavefront_breakdown"] = breakdown
     print(json.dumps(line))
     r.close()
     if dist:

@@ -271,6 +271,11 @@ typedef struct lgpu_stats {
     uint32_t node_bytes;      /* size of one BVH node record */
     uint32_t tri_record_bytes;/* size of one triangle record */
     uint64_t device_bytes;    /* device memory held by the committed scene */
+    /* wavefront breakdown of the last render, filled when the environment variable
+     * LGPU_PROFILE is set (events around every launch): */
+    double trace_ms, shade_ms, spawn_ms;
+    uint32_t iterations;      /* trace + resume rounds of the last wavefront render */
+    uint32_t pool_slots;
 } lgpu_stats;
 
 typedef struct lgpu_context lgpu_context;

@@ -88,7 +88,9 @@ class Stats(C.Structure):
     _fields_ = [("last_render_ms", C.c_double), ("paths", C.c_uint64), ("rays", C.c_uint64),
                 ("nodes_visited", C.c_uint64), ("tris_tested", C.c_uint64), ("bvh_nodes", C.c_uint64),
                 ("bvh_bytes", C.c_uint64), ("tri_bytes", C.c_uint64), ("node_bytes", C.c_uint32),
-                ("tri_record_bytes", C.c_uint32), ("device_bytes", C.c_uint64)]
+                ("tri_record_bytes", C.c_uint32), ("device_bytes", C.c_uint64),
+                ("trace_ms", C.c_double), ("shade_ms", C.c_double), ("spawn_ms", C.c_double),
+                ("iterations", C.c_uint32), ("pool_slots", C.c_uint32)]
 
 
 def render_opts(width, height, spp, max_bounces, min_bounces=3, seed=1, spectral=SPECTRAL_RGB3,

@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -47,6 +48,7 @@ struct lgpu_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     /* wavefront pool */
     void *w_states = nullptr;
+    void *w_cold = nullptr;
     size_t w_state_bytes = 0;
     size_t w_slots = 0;
     float4 *w_qo = nullptr, *w_qd = nullptr, *w_res = nullptr;
@@ -233,10 +235,11 @@ bool validate_scene(const HostScene &H, std::string &why) {
     }
     if ((size_t)S.power_cdf_off + 2 * H.lights.size() + 1 > fp) { why = "power cdf"; return false; }
     if (S.light_strategy == LGPU_LIGHT_STRATEGY_TREE && !H.lnodes.empty()) {
-        if (S.tree_root < 0 || (size_t)S.tree_root >= H.lnodes.size()) { why = "tree root"; return false; }
-        for (const DLNode &n : H.lnodes) {
-            if (n.child0 >= (int)H.lnodes.size() || n.child1 >= (int)H.lnodes.size() || n.parent >= (int)H.lnodes.size()) { why = "tree links"; return false; }
-            if ((n.child0 < 0) != (n.child1 < 0)) { why = "tree node with one child"; return false; }
+        if (S.tree_root != 1 || H.lnodes.size() < 2) { why = "tree root"; return false; }
+        for (size_t k = 1; k < H.lnodes.size(); ++k) {
+            const DLNode &n = H.lnodes[k];
+            if (n.child0 == 0 || n.child0 + 1 >= (int)H.lnodes.size() || n.parent == 0 || n.parent >= (int)H.lnodes.size()) { why = "tree links"; return false; }
+            if (n.child0 > 0 && (n.child0 & 1)) { why = "tree sibling pair alignment"; return false; }
             if (n.first < 0 || n.num < 1 || n.first + n.num > (int)H.treeLights.size()) { why = "tree light range"; return false; }
             if (n.child0 < 0 && (n.dist_off < 0 || (size_t)n.dist_off + 2 * n.num + 1 > fp)) { why = "tree leaf cdf"; return false; }
         }
@@ -294,7 +297,7 @@ LGPU_API void lgpu_destroy(lgpu_context *c) {
     cudaFree(c->d_ids);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
-    cudaFree(c->w_states); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
+    cudaFree(c->w_states); cudaFree(c->w_cold); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
     cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_counts); cudaFree(c->w_next); cudaFree(c->w_paths); cudaFree(c->w_free);
     if (c->h_count) cudaFreeHost(c->h_count);
     delete c;
@@ -731,7 +734,7 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
         std::vector<int2> slotOfInput(treeIn.size(), make_int2(-1, -1));
         for (size_t ni = 0; ni < lnodes.size(); ++ni) {
             const DLNode &n = lnodes[ni];
-            if (n.child0 >= 0) continue;
+            if (ni == 0 || n.child0 >= 0) continue;
             for (int k = 0; k < n.num; ++k) slotOfInput[to.order[n.first + k]] = make_int2((int)ni, k);
         }
         /* tree_slot is indexed by: mesh lights -> tri_base + tri, other lights -> their slot index */
@@ -742,6 +745,7 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
             else { lightSlot[r.x] = (int)k; treeSlot[k] = slotOfInput[k]; }
         }
         if (treeIn.empty() && envLight < 0) return fail(c, LGPU_ERR_INVALID_SCENE, "light tree is empty");
+        if (!treeIn.empty() && to.root < 0) return fail(c, LGPU_ERR_INVALID_SCENE, "light tree builder produced unpaired children");
     }
 
     /* ---------------- media */
@@ -830,13 +834,16 @@ int check_opts(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_o
 }
 
 /* Grow the wavefront pool to `slots` path slots of `state_bytes` each. */
-int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes) {
+int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes, size_t cold_bytes) {
     if (c->w_slots >= slots && c->w_state_bytes == state_bytes) return LGPU_OK;
+    cudaFree(c->w_cold);
+    c->w_cold = nullptr;
     cudaFree(c->w_states); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
     cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_free);
     c->w_states = nullptr; c->w_qo = c->w_qd = c->w_res = nullptr; c->w_resobj = c->w_qa = c->w_qb = c->w_free = nullptr;
     c->w_slots = 0;
     cudaError_t e = cudaMalloc(&c->w_states, slots * state_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_cold, slots * cold_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->w_qo, slots * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_qd, slots * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_res, slots * sizeof(float4));
@@ -860,10 +867,11 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
                   uint64_t base, uint64_t n, float4 *paths_out, bool count, cudaStream_t st) {
     const bool hero = o->spectral_mode == LGPU_SPECTRAL_HERO4;
     const size_t sb = hero ? wave_state_bytes_4_0() : wave_state_bytes_3_0();
+    const size_t cbytes = hero ? wave_cold_bytes_4_0() : wave_cold_bytes_3_0();
     const size_t want = o->pool_slots > 0 ? (size_t)o->pool_slots : ((size_t)4 << 20);
     const size_t slots = (size_t)std::min<uint64_t>(n, want);
     if (slots == 0) return LGPU_OK;
-    int rc = ensure_pool(c, slots, sb);
+    int rc = ensure_pool(c, slots, sb, cbytes);
     if (rc) return rc;
     WaveArgs W;
     std::memset(&W, 0, sizeof(W));
@@ -872,6 +880,7 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     W.rp.spp = o->spp; W.rp.max_bounces = o->max_bounces; W.rp.min_bounces = o->min_bounces;
     W.rp.seed = o->seed; W.rp.sample_offset = o->sample_offset;
     W.states = c->w_states;
+    W.cold = c->w_cold;
     W.qo = c->w_qo; W.qd = c->w_qd; W.res = c->w_res; W.res_obj = c->w_resobj;
     W.next_path = c->w_next;
     W.n_paths = n;
@@ -896,6 +905,10 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     cudaError_t e = resume((int)slots, 2);
     if (e != cudaSuccess) return cuda_fail(c, e, "wavefront start");
     int iters = 0;
+    static const bool prof = std::getenv("LGPU_PROFILE") != nullptr;
+    cudaEvent_t pe[4] = {nullptr, nullptr, nullptr, nullptr};
+    double acc[3] = {0, 0, 0};
+    if (prof) for (auto &x : pe) cudaEventCreate(&x);
     for (;;) {
         cudaMemcpyAsync(c->h_count, ca, LG_NSEG * sizeof(int), cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
@@ -907,14 +920,30 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
         if (++iters > 100000) return fail(c, LGPU_ERR_TIMEOUT, "wavefront did not drain");
         cudaMemsetAsync(cb, 0, LG_NSEG * sizeof(int), st);
         W.queue_in = qa; W.queue_out = qb; W.count_out = cb;
+        if (prof) cudaEventRecord(pe[0], st);
         e = count ? wave_trace_3_1(W, m, st) : wave_trace_3_0(W, m, st);
+        if (prof) cudaEventRecord(pe[1], st);
         if (e == cudaSuccess) e = resume(m, 0);
+        if (prof) cudaEventRecord(pe[2], st);
         if (e == cudaSuccess) e = resume(m, 1);   /* spawn into the slots freed by this resume */
+        if (prof) {
+            cudaEventRecord(pe[3], st);
+            cudaEventSynchronize(pe[3]);
+            float t0 = 0, t1 = 0, t2 = 0;
+            cudaEventElapsedTime(&t0, pe[0], pe[1]);
+            cudaEventElapsedTime(&t1, pe[1], pe[2]);
+            cudaEventElapsedTime(&t2, pe[2], pe[3]);
+            acc[0] += t0; acc[1] += t1; acc[2] += t2;
+        }
         if (e != cudaSuccess) return cuda_fail(c, e, "wavefront iteration");
         std::swap(qa, qb);
         std::swap(ca, cb);
     }
     c->last_iterations = iters;
+    c->stats.iterations += (uint32_t)iters;
+    c->stats.pool_slots = (uint32_t)slots;
+    c->stats.trace_ms += acc[0]; c->stats.shade_ms += acc[1]; c->stats.spawn_ms += acc[2];
+    if (prof) for (auto &x : pe) cudaEventDestroy(x);
     return LGPU_OK;
 }
 
@@ -960,6 +989,8 @@ int wavefront_frame(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_ren
 
 int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o, float4 *film, float4 *paths,
                 const uint64_t *ids, uint64_t n, bool count, cudaStream_t s) {
+    c->stats.trace_ms = c->stats.shade_ms = c->stats.spawn_ms = 0;
+    c->stats.iterations = 0;
     if (use_wavefront(o)) {
         if (count) cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
         cudaEventRecord(c->ev0, s);

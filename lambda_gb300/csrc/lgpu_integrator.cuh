@@ -335,10 +335,9 @@ struct Tracer {
 
     /* ---------------------------------------------------------------- light samplers */
     /* ManyLightSampler::ImportanceMeasure (ManyLightSampler.cpp:305-326) */
-    __device__ float importance(float3 p, float3 nS, const DLNode &n) {
-        const float3 cen = n.bmin + (n.bmax - n.bmin) * .5f;
-        float3 delta = cen - p;
-        const float diam = mag(n.bmax - n.bmin);
+    __device__ __forceinline__ float importance(float3 p, float3 nS, const DLNode &n) {
+        float3 delta = n.center - p;
+        const float diam = n.diag;
         const float d2 = dot(delta, delta);
         const float dd = sqrtf(d2);
         const float invD = 1.f / dd;
@@ -382,12 +381,13 @@ struct Tracer {
                     *pdf *= S.fpool[n.dist_off + n.num + 1 + off] / (n.integral * (float)n.num);
                     return tree_light_ref(n.first + off);
                 }
-                const float IL = importance(p, nS, S.lnodes[n.child0]);
-                const float IR = importance(p, nS, S.lnodes[n.child1]);
+                const DLNode cl = S.lnodes[n.child0], cr = S.lnodes[n.child0 + 1];
+                const float IL = importance(p, nS, cl);
+                const float IR = importance(p, nS, cr);
                 const float PL = IL / (IL + IR);
                 const float PR = 1.f - PL;
                 if (e < PL) { e /= PL; *pdf *= PL; ni = n.child0; }
-                else { e = (e - PL) / PR; *pdf *= PR; ni = n.child1; }
+                else { e = (e - PL) / PR; *pdf *= PR; ni = n.child0 + 1; }
             }
         }
         *pdf *= 1.f - pTree;
@@ -416,8 +416,9 @@ struct Tracer {
         int ni = leaf.parent;
         while (ni >= 0 && depth < LG_MAX_TREE_DEPTH) {
             const DLNode &n = S.lnodes[ni];
-            const float IL = importance(p, nS, S.lnodes[n.child0]);
-            const float IR = importance(p, nS, S.lnodes[n.child1]);
+            const DLNode cl = S.lnodes[n.child0], cr = S.lnodes[n.child0 + 1];
+            const float IL = importance(p, nS, cl);
+            const float IR = importance(p, nS, cr);
             const float p0 = IL / (IL + IR);
             lev[depth++] = (child == n.child0) ? p0 : 1.f - p0;
             child = ni;

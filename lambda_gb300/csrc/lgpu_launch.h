@@ -45,6 +45,10 @@ cudaError_t wave_resume_4_1(const WaveArgs &W, int n, int start_new, cudaStream_
 cudaError_t wave_trace_3_0(const WaveArgs &W, int n, cudaStream_t st);
 cudaError_t wave_trace_3_1(const WaveArgs &W, int n, cudaStream_t st);
 size_t wave_state_bytes_3_0();
+size_t wave_cold_bytes_3_0();
+size_t wave_cold_bytes_4_0();
+size_t wave_cold_bytes_3_1();
+size_t wave_cold_bytes_4_1();
 size_t wave_state_bytes_4_0();
 size_t wave_state_bytes_3_1();
 size_t wave_state_bytes_4_1();

@@ -10,6 +10,7 @@
  */
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <limits>
 #include <vector>
 
@@ -243,25 +244,32 @@ void build_light_tree(const std::vector<TreeLightIn> &lights, std::vector<float>
     B.build(0);
     out.tree_power = B.treePower;
     out.order = B.order;
-    out.root = 0;
+    /* record k + 1 holds builder node k (record 0 unused): sibling pairs (2j+1, 2j+2) of the builder
+     * become records (2j+2, 2j+3), a 128-byte aligned pair */
+    out.root = 1;
+    out.nodes.resize(B.nodes.size() + 1);
+    std::memset(&out.nodes[0], 0, sizeof(DLNode));
+    out.nodes[0].child0 = -1;
+    out.nodes[0].parent = -1;
     for (size_t i = 0; i < B.nodes.size(); ++i) {
         const Node &n = B.nodes[i];
         DLNode d;
-        d.bmin = make_float3(n.b.mn.x, n.b.mn.y, n.b.mn.z);
-        d.bmax = make_float3(n.b.mx.x, n.b.mx.y, n.b.mx.z);
+        const V3f c = n.b.center();
+        d.center = make_float3(c.x, c.y, c.z);
+        d.diag = n.b.diagonal();
         d.axis = make_float3(n.cone.axis.x, n.cone.axis.y, n.cone.axis.z);
         d.thetaO = n.cone.thetaO;
         d.thetaE = n.cone.thetaE;
         d.power = n.power;
-        d.child0 = n.ch[0];
-        d.child1 = n.ch[1];
-        d.parent = n.parent;
+        d.child0 = n.ch[0] >= 0 ? n.ch[0] + 1 : -1;
+        d.parent = n.parent >= 0 ? n.parent + 1 : -1;
         d.first = (int)n.first;
         d.num = (int)n.num;
         d.dist_off = -1;
         d.integral = 0;
+        if (n.ch[0] >= 0 && n.ch[1] != n.ch[0] + 1) { out.root = -1; return; }   /* builder invariant */
         if (n.ch[0] < 0) d.integral = piecewise1d(n.leafPowers.data(), n.num, pool, d.dist_off);
-        out.nodes.push_back(d);
+        out.nodes[i + 1] = d;
     }
 }
 

@@ -150,51 +150,92 @@ cudaError_t LG_CAT(launch_render_, LGPU_NS, LGPU_COUNT)(const LaunchArgs &a) {
 
 /* ---------------------------------------------------------------- wavefront kernels */
 template <int NS, bool COUNT>
-__device__ __forceinline__ void wave_save(Wave<NS, COUNT> &w, PState<NS> &s) {
+__device__ __forceinline__ void wave_save(Wave<NS, COUNT> &w, PHot<NS> &s) {
     s.key = w.rng.key;
     s.dim = w.rng.dim;
 #pragma unroll
     for (int k = 0; k < 4; ++k) s.lam[k] = w.lam.l[k];
 }
 
+/* Warp-cooperative copy of the 32 lanes' hot states between HBM and shared memory: for each lane's
+ * slot, the warp moves the whole record with consecutive 16-byte accesses (coalesced). */
+template <int NS>
+__device__ __forceinline__ void warp_stage(PHot<NS> *G, PHot<NS> *sh, int slot, bool to_shared) {
+    constexpr int W4 = (int)(sizeof(PHot<NS>) / sizeof(float4));
+    const int lane = threadIdx.x & 31;
+#pragma unroll 1
+    for (int j = 0; j < 32; ++j) {
+        const int sj = __shfl_sync(0xffffffffu, slot, j);
+        if (sj < 0) continue;
+        float4 *g = reinterpret_cast<float4 *>(G + sj);
+        float4 *l = reinterpret_cast<float4 *>(sh + j);
+        for (int k = lane; k < W4; k += 32) {
+            if (to_shared) l[k] = g[k];
+            else g[k] = l[k];
+        }
+    }
+    __syncwarp();
+}
+
 /* Continue every slot of the (segmented) input queue until its next query or its end. */
 template <int NS, bool COUNT>
 __global__ void __launch_bounds__(128) k_wave_resume(WaveArgs W, int n) {
+    extern __shared__ float4 smem4[];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int seg = 0;
+    int slot = -1;
+    if (i < n) {
+        int seg = 0;
 #pragma unroll
-    for (int k = 1; k < LG_NSEG; ++k) seg += (i >= W.seg_off[k]) ? 1 : 0;
-    const int slot = W.queue_in[seg * W.cap + (i - W.seg_off[seg])];
-    PState<NS> &s = reinterpret_cast<PState<NS> *>(W.states)[slot];
-    Wave<NS, COUNT> w{W, s, slot};
-    w.rng.key = s.key;
-    w.rng.dim = s.dim;
+        for (int k = 1; k < LG_NSEG; ++k) seg += (i >= W.seg_off[k]) ? 1 : 0;
+        slot = W.queue_in[seg * W.cap + (i - W.seg_off[seg])];
+    }
+    PHot<NS> *G = reinterpret_cast<PHot<NS> *>(W.states);
+    PHot<NS> *sh = reinterpret_cast<PHot<NS> *>(smem4) + (threadIdx.x & ~31);
+    warp_stage<NS>(G, sh, slot, true);
+    int keep = -1;
+    if (slot >= 0) {
+        PHot<NS> &s = sh[threadIdx.x & 31];
+        PCold<NS> &c = reinterpret_cast<PCold<NS> *>(W.cold)[slot];
+        Wave<NS, COUNT> w{W, s, c, slot};
+        w.rng.key = s.key;
+        w.rng.dim = s.dim;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) w.lam.l[k] = s.lam[k];
-    w.run();
-    if (s.pc == PC_DONE) { w.finish(); push_free(W, slot); return; }
-    wave_save(w, s);
+        for (int k = 0; k < 4; ++k) w.lam.l[k] = s.lam[k];
+        w.run();
+        if (s.pc == PC_DONE) { w.finish(); push_free(W, slot); }
+        else { wave_save(w, s); keep = slot; }
+    }
+    __syncwarp();
+    warp_stage<NS>(G, sh, keep, false);
 }
 
 /* Start new paths in free slots: consecutive path ids go to consecutive free-list entries, so the
  * warps of a spawn trace neighbouring samples of one pixel.  Slots come from the free list, or from
- * the untouched tail of the pool on the first spawn (free_list == nullptr). */
+ * the untouched tail of the pool on the first spawn. */
 template <int NS, bool COUNT>
 __global__ void __launch_bounds__(128) k_wave_spawn(WaveArgs W, int n_max, int fresh) {
+    extern __shared__ float4 smem4[];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nfree = fresh ? n_max : *W.free_count;
     const unsigned long long next = *W.next_path;
     const unsigned long long left = next < W.n_paths ? W.n_paths - next : 0ull;
     const int m = (int)(nfree < (int)min(left, (unsigned long long)0x7fffffff) ? nfree : (int)left);
-    if (i >= m) return;
-    const int slot = fresh ? i : W.free_list[i];
-    PState<NS> &s = reinterpret_cast<PState<NS> *>(W.states)[slot];
-    Wave<NS, COUNT> w{W, s, slot};
-    w.start_path(next + (uint64_t)i);
-    w.run();
-    if (s.pc == PC_DONE) { w.finish(); return; }   /* slot idles until the next spawn reuses it */
-    wave_save(w, s);
+    if (blockIdx.x * blockDim.x >= m) return;   /* whole block idle */
+    int keep = -1;
+    PHot<NS> *G = reinterpret_cast<PHot<NS> *>(W.states);
+    PHot<NS> *sh = reinterpret_cast<PHot<NS> *>(smem4) + (threadIdx.x & ~31);
+    if (i < m) {
+        const int slot = fresh ? i : W.free_list[i];
+        PHot<NS> &s = sh[threadIdx.x & 31];
+        PCold<NS> &c = reinterpret_cast<PCold<NS> *>(W.cold)[slot];
+        Wave<NS, COUNT> w{W, s, c, slot};
+        w.start_path(next + (uint64_t)i);
+        w.run();
+        if (s.pc == PC_DONE) w.finish();   /* slot idles until a later spawn reuses it */
+        else { wave_save(w, s); keep = slot; }
+    }
+    __syncwarp();
+    warp_stage<NS>(G, sh, keep, false);
 }
 /* next_path += paths started by the last spawn; clear the free list. */
 static __global__ void k_wave_advance(WaveArgs W, int n_max, int fresh) {
@@ -207,17 +248,25 @@ static __global__ void k_wave_advance(WaveArgs W, int n_max, int fresh) {
 }
 
 cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, int start_new, cudaStream_t st) {
+    const size_t smem = 128 * sizeof(PHot<LGPU_NS>);
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(k_wave_resume<LGPU_NS, LGPU_COUNT != 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_wave_spawn<LGPU_NS, LGPU_COUNT != 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = true;
+    }
     if (start_new) {
         /* spawn into up to n slots (fresh pool or free list), then advance the path counter */
-        if (n > 0) k_wave_spawn<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, 0, st>>>(W, n, start_new == 2);
+        if (n > 0) k_wave_spawn<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, smem, st>>>(W, n, start_new == 2);
         k_wave_advance<<<1, 1, 0, st>>>(W, n, start_new == 2);
         return cudaGetLastError();
     }
     if (n <= 0) return cudaSuccess;
-    k_wave_resume<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, 0, st>>>(W, n);
+    k_wave_resume<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, smem, st>>>(W, n);
     return cudaGetLastError();
 }
-size_t LG_CAT(wave_state_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PState<LGPU_NS>); }
+size_t LG_CAT(wave_state_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PHot<LGPU_NS>); }
+size_t LG_CAT(wave_cold_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PCold<LGPU_NS>); }
 
 #if LGPU_NS == 3
 /* Answer every queued query: closest hit (Scene::Intersect) or occlusion (rtcOccluded1). */

@@ -105,12 +105,18 @@ struct DLight {
     float pad;
 };
 
-/* Flattened ManyLightSampler node (ManyLightSampler.h:47-60). */
-struct DLNode {
-    float3 bmin, bmax;
+/* Flattened ManyLightSampler node (ManyLightSampler.h:47-60), 64 bytes.  Bounds are stored as the
+ * centre and diagonal length the importance measure uses (Bounds::Center / DiagonalLength,
+ * evaluated on the host with the reference's float operations).  Children are consecutive records
+ * (child1 = child0 + 1) and sibling pairs start on a 128-byte boundary, so one line fetch serves
+ * both importance evaluations of a descent step.  Record 0 is unused; the root is record 1. */
+struct __align__(16) DLNode {
+    float3 center;
+    float diag;
     float3 axis;
-    float thetaO, thetaE, power;
-    int child0, child1, parent;
+    float thetaO;
+    float thetaE, power;
+    int child0, parent;
     int first, num;      /* light range in tree order */
     int dist_off;        /* leaf: CDF (num+1) then raw powers (num) in fpool */
     float integral;      /* leaf CDF integral */

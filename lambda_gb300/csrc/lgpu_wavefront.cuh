@@ -2,7 +2,7 @@
  * Wavefront form of MISVolumetricPathIntegrator::Li (src/integrators/MISVolumetricPathIntegrator.cpp:23-215).
  *
  * The integrator is cut at every ray query into a resumable state machine.  A pool of path slots
- * lives in HBM (PState, one per slot); each iteration of the host loop runs
+ * lives in HBM (PHot + PCold, one per slot); each iteration of the host loop runs
  *   k_trace   -- every pending query (closest hit or occlusion) with a small, register-light
  *                traversal kernel, queries read from a compacted queue;
  *   k_resume  -- every slot with an answered query continues its path until it issues the next
@@ -47,8 +47,11 @@ __host__ __device__ __forceinline__ int seg_of(int pc) {
 }
 enum : int { TR_TEMP = 0, TR_EVENT = 1 };
 
+/* Per-slot path state.  The hot part (everything a surface bounce touches) is staged through
+ * shared memory by k_resume with coalesced warp copies; the cold part (medium bounce and the
+ * IntersectTr sub-machine) stays in HBM and is only touched by paths inside participating media. */
 template <int NS>
-struct PState {
+struct __align__(16) PHot {
     uint64_t out;                 /* output index of the path (within the chunk) */
     uint32_t key, dim;
     uint32_t pixel, pad0;
@@ -60,37 +63,43 @@ struct PState {
     Event ev;
     /* surface bounce */
     LRef l;
-    float lightDistPdf, scatteringPDF, lightPDF, pad1;
+    float lightDistPdf, scatteringPDF, lightPDF, lsSinT;
     float3 sp, sn;
-    Spec<NS> Ld, f, Li;
+    Spec<NS> Ld, f;
     float3 lsP;                   /* light point (area/point) or env (u, v) */
     int lsT;                      /* sampled triangle of a mesh light */
-    float lsSinT;
+    /* visibility sub-machine */
+    int visRet, visMode, visOK;
+    float visM;
+    Spec<NS> trTr;                /* transmittance of the last visibility / IntersectTr query */
+    float tmpTFar;
+    int trResult;
+    int pad1, pad2;
+};
+template <int NS>
+struct __align__(16) PCold {
     /* medium bounce */
     LRef ml;
     float3 mPoint, mNormal;
     Spec<NS> mLe;
     float mPdf;
-    int choice, mk;
+    int choice, medK;
     float distT, distPdf, eqT, eqPdf, distW, eqW;
     Spec<NS> mTrD, mTrE, mLd, kLd;
     float3 mpD, mpE, wiD, wiE;
     float kPartial, kPhasePdf;
-    /* visibility sub-machine */
-    int visRet, visMode, visOK;
-    float visM;
     /* IntersectTr sub-machine */
-    int trRet, trTarget, trMed, trIter, trResult;
-    float trTFar, trMaxT, tmpTFar;
+    int trRet, trTarget, trMed, trIter;
+    float trTFar, trMaxT;
     float3 trO, trD;
-    Spec<NS> trTr;
 };
 
 struct WaveArgs {
     DeviceScene S;
     CamParams cam;
     RenderParams rp;
-    void *states;
+    void *states;                 /* PHot per slot */
+    void *cold;                   /* PCold per slot */
     float4 *qo, *qd;              /* per slot: origin + tmax, direction + query type */
     float4 *res;                  /* per slot: t, u, v, prim (closest) or occluded flag */
     int *res_obj;
@@ -130,7 +139,8 @@ __device__ __forceinline__ void push_free(const WaveArgs &W, int slot) {
 template <int NS, bool COUNT>
 struct Wave {
     const WaveArgs &W;
-    PState<NS> &s;
+    PHot<NS> &s;
+    PCold<NS> &c;
     int slot;
     Rng rng;
     Lambda4 lam;
@@ -154,8 +164,8 @@ struct Wave {
 
     /* ---- sub-machines ---- */
     __device__ void start_tr(float3 o, float3 d, int med, int target, float maxT, int ret) {
-        s.trO = o; s.trD = d; s.trMed = med; s.trTarget = target; s.trMaxT = maxT; s.trRet = ret;
-        s.trTFar = 0.f; s.trIter = 0; s.trTr = Spec<NS>(1.f);
+        c.trO = o; c.trD = d; c.trMed = med; c.trTarget = target; c.trMaxT = maxT; c.trRet = ret;
+        c.trTFar = 0.f; c.trIter = 0; s.trTr = Spec<NS>(1.f);
         if (target == TR_TEMP) s.tmpTFar = finf();
         issue(o, d, finf(), Q_CLOSEST, PC_TR_STEP);
     }
@@ -270,41 +280,41 @@ struct Wave {
     /* Light::Visibility for a medium point (LdMediumPoint): query part */
     __device__ void ldm_vis_prepare(float3 p) {
         const DeviceScene &S = W.S;
-        if (s.ml.light < 0) { s.mPdf = 0.f; s.visOK = 0; s.pc = PC_LDM_VIS; s.visMode = -1; return; }
-        const DLight &L = S.lights[s.ml.light];
+        if (c.ml.light < 0) { c.mPdf = 0.f; s.visOK = 0; s.pc = PC_LDM_VIS; s.visMode = -1; return; }
+        const DLight &L = S.lights[c.ml.light];
         if (L.type == LT_ENV) {
-            const float3 wi = normalised(s.mPoint - p);
+            const float3 wi = normalised(c.mPoint - p);
             start_vis(p, wi, 0.f, VIS_ESCAPE, PC_LDM_VIS);
             return;
         }
         if (L.type == LT_POINT || L.type == LT_SPOT) {
             const float3 q = p + s.hit.nG * SURFACE_EPSILON * (float)s.ev.sidedness;
-            const float3 diff = s.mPoint - q;
+            const float3 diff = c.mPoint - q;
             const float m = mag(diff);
             s.ev.wi = divs(diff, m);
             start_vis(q, s.ev.wi, m, VIS_POINT, PC_LDM_VIS);
             return;
         }
-        const float3 diff = s.mPoint - p;
+        const float3 diff = c.mPoint - p;
         const float m = mag(diff);
         s.ev.wi = divs(diff, m);
         start_vis(p, s.ev.wi, m, VIS_AREA, PC_LDM_VIS);
     }
     __device__ Spec<NS> ldm_vis_complete(float3 p) {
         const DeviceScene &S = W.S;
-        if (s.ml.light < 0) { s.mPdf = 0.f; return Spec<NS>(0.f); }
-        const DLight &L = S.lights[s.ml.light];
+        if (c.ml.light < 0) { c.mPdf = 0.f; return Spec<NS>(0.f); }
+        const DLight &L = S.lights[c.ml.light];
         auto t = T();
         const Spec<NS> Tr = s.trTr;
-        if (!s.visOK) { s.mPdf = 0.f; return Spec<NS>(0.f); }
+        if (!s.visOK) { c.mPdf = 0.f; return Spec<NS>(0.f); }
         if (L.type == LT_ENV) return Tr;
         if (L.type == LT_POINT || L.type == LT_SPOT) {
             Spec<NS> v = Tr;
             if (L.type == LT_SPOT) v = v * t.spot_falloff(L, -s.ev.wi);
             return v / distsq(L.pos, s.hit.point);
         }
-        const float cT = s.ml.tri < 0 ? fabsf(dot(s.mNormal, -s.ev.wi)) : fabsf(dot(s.hit.nG, -s.ev.wi));
-        s.mPdf *= distsq(p, s.mPoint) / cT;
+        const float cT = c.ml.tri < 0 ? fabsf(dot(c.mNormal, -s.ev.wi)) : fabsf(dot(s.hit.nG, -s.ev.wi));
+        c.mPdf *= distsq(p, c.mPoint) / cT;
         return Tr;
     }
 
@@ -507,36 +517,36 @@ struct Wave {
             case PC_MED_A: {
                 auto t = T();
                 const DMedium &med = S.media[s.ev.medium];
-                s.mPdf = 1.f;
+                c.mPdf = 1.f;
                 s.sp = s.hit.point; s.sn = s.hit.nS;
                 float mp = 1.f;
-                s.ml = t.sample_light(s.hit.point, s.hit.nS, &mp);
+                c.ml = t.sample_light(s.hit.point, s.hit.nS, &mp);
                 float3 lp, ln = mk(0.f, 0.f, 0.f);
-                s.mLe = t.sample_point(s.ml, s.ev, s.hit, lp, ln, mp);
-                s.mPdf = mp; s.mPoint = lp; s.mNormal = ln;
-                s.choice = (rng.next() > 0.5f) ? 0 : 1;
+                c.mLe = t.sample_point(c.ml, s.ev, s.hit, lp, ln, mp);
+                c.mPdf = mp; c.mPoint = lp; c.mNormal = ln;
+                c.choice = (rng.next() > 0.5f) ? 0 : 1;
                 float distT, distPdf, eqT, eqPdf;
-                s.mTrD = medium_sample_distance<NS>(med, rng, s.ev, s.hit, &distT, &distPdf);
+                c.mTrD = medium_sample_distance<NS>(med, rng, s.ev, s.hit, &distT, &distPdf);
                 const bool intD = s.ev.mediumInteraction;
-                s.mTrE = medium_sample_equiangular<NS>(med, s.ro, s.rd, rng, s.ev, s.hit, s.mPoint, &eqT, &eqPdf);
+                c.mTrE = medium_sample_equiangular<NS>(med, s.ro, s.rd, rng, s.ev, s.hit, c.mPoint, &eqT, &eqPdf);
                 const bool intE = s.ev.mediumInteraction;
                 s.ev.mediumInteraction = intD && intE;
-                if (!s.ev.mediumInteraction) { s.beta *= s.mTrD; s.pc = PC_SURF_A; break; }
+                if (!s.ev.mediumInteraction) { s.beta *= c.mTrD; s.pc = PC_SURF_A; break; }
                 s.ev.wo = -s.rd;
-                s.mLd = Spec<NS>(0.f);
-                s.mpD = s.ro + s.rd * distT;
-                s.mpE = s.ro + s.rd * eqT;
+                c.mLd = Spec<NS>(0.f);
+                c.mpD = s.ro + s.rd * distT;
+                c.mpE = s.ro + s.rd * eqT;
                 const float distPdf2 = medium_pdf_distance<NS>(med, eqT);
-                const float eqPdf2 = medium_pdf_equiangular(s.ro, s.rd, s.mPoint, s.hit.tFar, distT);
-                s.distW = Tracer<NS, COUNT>::power_heuristic(distPdf, eqPdf2);
-                s.eqW = Tracer<NS, COUNT>::power_heuristic(eqPdf, distPdf2);
-                s.mk = 0;
+                const float eqPdf2 = medium_pdf_equiangular(s.ro, s.rd, c.mPoint, s.hit.tFar, distT);
+                c.distW = Tracer<NS, COUNT>::power_heuristic(distPdf, eqPdf2);
+                c.eqW = Tracer<NS, COUNT>::power_heuristic(eqPdf, distPdf2);
+                c.medK = 0;
                 s.pc = PC_LDM_START;
                 break;
             }
             case PC_LDM_START: {
-                const float3 p = s.mk == 0 ? s.mpD : s.mpE;
-                s.kPartial = s.mPdf;
+                const float3 p = c.medK == 0 ? c.mpD : c.mpE;
+                c.kPartial = c.mPdf;
                 s.hit.point = p;
                 ldm_vis_prepare(p);
                 if (s.pc != PC_LDM_VIS) return;   /* a query was issued */
@@ -545,9 +555,9 @@ struct Wave {
             case PC_LDM_VIS: {
                 auto t = T();
                 const DMedium &med = S.media[s.ev.medium];
-                const float3 p = s.mk == 0 ? s.mpD : s.mpE;
-                const Spec<NS> Li = s.mLe * ldm_vis_complete(p);
-                const float lightPDF = s.mPdf;
+                const float3 p = c.medK == 0 ? c.mpD : c.mpE;
+                const Spec<NS> Li = c.mLe * ldm_vis_complete(p);
+                const float lightPDF = c.mPdf;
                 Spec<NS> kLd(0.f);
                 if (lightPDF > 0.f && !Li.black()) {
                     const float sp = phase_hg(dot(s.ev.wo, s.ev.wi), med.g);
@@ -556,11 +566,11 @@ struct Wave {
                         kLd += Li * Spec<NS>(sp) * w / lightPDF;
                     }
                 }
-                s.kLd = kLd;
+                c.kLd = kLd;
                 float3 wi;
-                s.kPhasePdf = hg_sample(med.g, s.ev.wo, &wi, rng);
+                c.kPhasePdf = hg_sample(med.g, s.ev.wo, &wi, rng);
                 s.ev.wi = wi;
-                if (s.mk == 0) s.wiD = wi; else s.wiE = wi;
+                if (c.medK == 0) c.wiD = wi; else c.wiE = wi;
                 start_tr(p, wi, s.ev.medium, TR_EVENT, -1.f, PC_LDM_SCAT);
                 return;
             }
@@ -568,21 +578,21 @@ struct Wave {
                 auto t = T();
                 const bool hs = s.trResult != 0;
                 const Spec<NS> Tr = s.trTr;
-                Spec<NS> kLd = s.kLd;
-                if (s.kPhasePdf > 0.f) {
+                Spec<NS> kLd = c.kLd;
+                if (c.kPhasePdf > 0.f) {
                     LRef nl; nl.light = hs ? t.mat(s.hit).light : S.env_light; nl.tri = -1;
                     if (nl.light >= 0) {
-                        if (!lref_eq(nl, s.ml)) s.kPartial = t.light_pdf(s.sp, s.sn, s.hit.prim, nl);
-                        const float lightPDF = s.kPartial * t.pdf_li(nl, s.ev, s.hit);
+                        if (!lref_eq(nl, c.ml)) c.kPartial = t.light_pdf(s.sp, s.sn, s.hit.prim, nl);
+                        const float lightPDF = c.kPartial * t.pdf_li(nl, s.ev, s.hit);
                         const Spec<NS> Li = hs ? t.light_L(nl, s.ev, s.hit) : t.light_Le(nl, s.ev.wi);
-                        const float w = Tracer<NS, COUNT>::power_heuristic(s.kPhasePdf, lightPDF);
-                        if (!Li.black() && lightPDF > 0.f) kLd += Li * Tr * w / s.kPhasePdf;
+                        const float w = Tracer<NS, COUNT>::power_heuristic(c.kPhasePdf, lightPDF);
+                        if (!Li.black() && lightPDF > 0.f) kLd += Li * Tr * w / c.kPhasePdf;
                     }
                 }
-                if (s.mk == 0) { s.mLd += kLd * s.mTrD * s.distW; s.mk = 1; s.pc = PC_LDM_START; break; }
-                s.mLd += kLd * s.mTrE * s.eqW;
-                s.ro = s.choice == 0 ? s.mpD : s.mpE;
-                s.rd = s.choice == 0 ? s.wiD : s.wiE;
+                if (c.medK == 0) { c.mLd += kLd * c.mTrD * c.distW; c.medK = 1; s.pc = PC_LDM_START; break; }
+                c.mLd += kLd * c.mTrE * c.eqW;
+                s.ro = c.choice == 0 ? c.mpD : c.mpE;
+                s.rd = c.choice == 0 ? c.wiD : c.wiE;
                 issue(s.ro, s.rd, finf(), Q_CLOSEST, PC_MED_EXT);
                 return;
             }
@@ -591,8 +601,8 @@ struct Wave {
                 const bool ok = closest(hr);
                 if (ok) process_hit(S, s.ro, s.rd, hr, s.hit);
                 s.scatterIntersect = ok;
-                s.L += s.mLd;
-                s.beta *= (s.choice == 0 ? s.mTrD : s.mTrE);
+                s.L += c.mLd;
+                s.beta *= (c.choice == 0 ? c.mTrD : c.mTrE);
                 s.pc = PC_RR;
                 break;
             }
@@ -611,30 +621,30 @@ struct Wave {
             case PC_TR_STEP: {   /* one segment of Scene::IntersectTr (Scene.cpp:45-81) */
                 auto t = T();
                 HitRec hr;
-                if (!closest(hr)) { s.trResult = 0; s.pc = s.trRet; break; }
+                if (!closest(hr)) { s.trResult = 0; s.pc = c.trRet; break; }
                 RayHit tmp;
-                RayHit &h = s.trTarget == TR_EVENT ? s.hit : tmp;
-                process_hit(S, s.trO, s.trD, hr, h);
-                if (s.trTarget == TR_TEMP) s.tmpTFar = h.tFar;
-                s.trTFar += h.tFar;
+                RayHit &h = c.trTarget == TR_EVENT ? s.hit : tmp;
+                process_hit(S, c.trO, c.trD, hr, h);
+                if (c.trTarget == TR_TEMP) s.tmpTFar = h.tFar;
+                c.trTFar += h.tFar;
                 bool term = false;
-                if (s.trMaxT >= 0.f) {
-                    term = s.trTFar > s.trMaxT;
-                    if (term) { const float delta = s.trTFar - s.trMaxT; s.trTFar -= delta; h.tFar -= delta; }
+                if (c.trMaxT >= 0.f) {
+                    term = c.trTFar > c.trMaxT;
+                    if (term) { const float delta = c.trTFar - c.trMaxT; c.trTFar -= delta; h.tFar -= delta; }
                 }
-                if (s.trMed >= 0) s.trTr *= medium_tr<NS>(S.media[s.trMed], h.tFar);
+                if (c.trMed >= 0) s.trTr *= medium_tr<NS>(S.media[c.trMed], h.tFar);
                 const DMaterial &m = t.mat(h);
                 if (term || m.has_bsdf || m.light >= 0) {
-                    h.tFar = s.trTFar;
-                    if (s.trTarget == TR_TEMP) s.tmpTFar = s.trTFar;
+                    h.tFar = c.trTFar;
+                    if (c.trTarget == TR_TEMP) s.tmpTFar = c.trTFar;
                     s.trResult = 1;
-                    s.pc = s.trRet;
+                    s.pc = c.trRet;
                     break;
                 }
-                s.trMed = t.get_medium(m, s.trD, h.nG);
-                s.trO = h.point + h.nG * (dot(h.nG, s.trD) < 0.f ? -SURFACE_EPSILON : SURFACE_EPSILON);
-                if (++s.trIter >= 256) { s.trResult = 0; s.pc = s.trRet; break; }
-                issue(s.trO, s.trD, finf(), Q_CLOSEST, PC_TR_STEP);
+                c.trMed = t.get_medium(m, c.trD, h.nG);
+                c.trO = h.point + h.nG * (dot(h.nG, c.trD) < 0.f ? -SURFACE_EPSILON : SURFACE_EPSILON);
+                if (++c.trIter >= 256) { s.trResult = 0; s.pc = c.trRet; break; }
+                issue(c.trO, c.trD, finf(), Q_CLOSEST, PC_TR_STEP);
                 return;
             }
             case PC_DONE:
