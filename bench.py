@@ -221,6 +221,12 @@ def main():
     torch.cuda.synchronize()
     total_ms = t_start.elapsed_time(t_end)
     kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    # every path of every rendered frame must have reached the film (no work skipped)
+    rendered = args.warmup + args.steps + (1 if os.environ.get("LGPU_PROFILE") else 0)
+    counts = film[..., 3]
+    if not bool(torch.all(counts == float(spp * rendered))):
+        raise SystemExit("work check failed: film sample counts %s, expected %d per pixel"
+                         % (torch.unique(counts)[:8].tolist(), spp * rendered))
     # end to end through the host-buffer API (film copies inside the timed region)
     host_film = np.zeros((H, W, 4), np.float32)
     torch.cuda.synchronize()

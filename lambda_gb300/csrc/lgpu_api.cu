@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdlib>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -579,6 +580,7 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
             if (ld.emission_node < 0 || ld.emission_node >= d->num_nodes) return fail(c, LGPU_ERR_INVALID_SCENE, "light " + std::to_string(i) + " has no emission socket");
             if (!gc.compile_emission(ld.emission_node, ld.emission_socket, L.prog_off, L.prog_len, L.out_reg))
                 return fail(c, LGPU_ERR_UNSUPPORTED_NODE, "light " + std::to_string(i) + ": " + gc.err);
+            L.em_folded = gc.fold_emission(L.prog_off, L.prog_len, L.out_reg, L.em) ? 1 : 0;
         }
         if (ld.type == LGPU_LIGHT_MESH) {
             if (ld.object < 0 || ld.object >= d->num_objects) return fail(c, LGPU_ERR_INVALID_SCENE, "mesh light without object");
@@ -745,7 +747,9 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
             else { lightSlot[r.x] = (int)k; treeSlot[k] = slotOfInput[k]; }
         }
         if (treeIn.empty() && envLight < 0) return fail(c, LGPU_ERR_INVALID_SCENE, "light tree is empty");
-        if (!treeIn.empty() && to.root < 0) return fail(c, LGPU_ERR_INVALID_SCENE, "light tree builder produced unpaired children");
+        if (!treeIn.empty() && to.root < 0)
+            return fail(c, LGPU_ERR_INVALID_SCENE, to.root == -2 ? "light-tree cone with an emission angle other than pi/2"
+                                                                 : "light tree builder produced unpaired children");
     }
 
     /* ---------------- media */
@@ -889,6 +893,7 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     W.path_out = paths_out;
     W.counters = c->d_counters;
     W.cap = (int)slots;
+    W.cap_in = (int)slots;
     W.free_list = c->w_free;
     auto resume = [&](int m, int mode) {
         if (hero) return count ? wave_resume_4_1(W, m, mode, st) : wave_resume_4_0(W, m, mode, st);
@@ -906,6 +911,8 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     if (e != cudaSuccess) return cuda_fail(c, e, "wavefront start");
     int iters = 0;
     static const bool prof = std::getenv("LGPU_PROFILE") != nullptr;
+    static const bool prof_seg = prof && std::string(std::getenv("LGPU_PROFILE")) == "2";
+    static double seg_ms[LG_NSEG] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t pe[4] = {nullptr, nullptr, nullptr, nullptr};
     double acc[3] = {0, 0, 0};
     if (prof) for (auto &x : pe) cudaEventCreate(&x);
@@ -923,7 +930,33 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
         if (prof) cudaEventRecord(pe[0], st);
         e = count ? wave_trace_3_1(W, m, st) : wave_trace_3_0(W, m, st);
         if (prof) cudaEventRecord(pe[1], st);
-        if (e == cudaSuccess) e = resume(m, 0);
+        if (e == cudaSuccess) {
+            /* one resume launch per queue segment: each launch enters the state machine at one
+             * program point, so its warps run the same code (timed separately with LGPU_PROFILE=2) */
+            WaveArgs W0 = W;
+            for (int k = 0; k < LG_NSEG && e == cudaSuccess; ++k) {
+                const int nk = W.seg_off[k + 1] - W.seg_off[k];
+                if (nk <= 0) continue;
+                for (int j = 0; j <= LG_NSEG; ++j) W.seg_off[j] = j <= k ? 0 : 0x7fffffff;
+                W.queue_in = qa + (size_t)k * W.cap;
+                W.cap_in = 0;
+                if (prof_seg) {
+                    cudaEvent_t a, b;
+                    cudaEventCreate(&a); cudaEventCreate(&b);
+                    cudaEventRecord(a, st);
+                    e = resume(nk, 0);
+                    cudaEventRecord(b, st);
+                    cudaEventSynchronize(b);
+                    float t = 0;
+                    cudaEventElapsedTime(&t, a, b);
+                    seg_ms[k] += t;
+                    cudaEventDestroy(a); cudaEventDestroy(b);
+                } else {
+                    e = resume(nk, 0);
+                }
+                W = W0;
+            }
+        }
         if (prof) cudaEventRecord(pe[2], st);
         if (e == cudaSuccess) e = resume(m, 1);   /* spawn into the slots freed by this resume */
         if (prof) {
@@ -944,6 +977,11 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     c->stats.pool_slots = (uint32_t)slots;
     c->stats.trace_ms += acc[0]; c->stats.shade_ms += acc[1]; c->stats.spawn_ms += acc[2];
     if (prof) for (auto &x : pe) cudaEventDestroy(x);
+    if (prof_seg) {
+        std::fprintf(stderr, "[lgpu] resume ms per segment (top_hit surf_ext null_ext med_ext vis_occl tr_step):");
+        for (int k = 0; k < LG_NSEG; ++k) { std::fprintf(stderr, " %.1f", seg_ms[k]); seg_ms[k] = 0; }
+        std::fprintf(stderr, "\n");
+    }
     return LGPU_OK;
 }
 

@@ -35,6 +35,10 @@ struct GraphCompiler {
     /* compile a light's emission socket; out_reg receives the illuminant spectrum register,
      * out_reg + 1 the reflectance one */
     bool compile_emission(int node, int socket, int &prog_off, int &prog_len, int &out_reg);
+    /* RGB-mode constant folding of context-free programs */
+    bool context_free(int off, int len) const;
+    void fold_material(DMaterial &m);
+    bool fold_emission(int prog_off, int prog_len, int out_reg, float4 em[2]);
 };
 
 }  // namespace lg

@@ -513,7 +513,34 @@ bool GraphCompiler::compile_material(int bxdf_node, DMaterial &m) {
         m.leaves[i].rough = (uint8_t)(lv[i].rough >= 0 ? phys[lv[i].rough] : 0);
     }
     for (int i = 0; i < m.num_tree; ++i) m.tree[i].ratio = (uint8_t)(ratioV[i] >= 0 ? phys[ratioV[i]] : 0);
+    fold_material(m);
     return true;
+}
+
+/* Does a program read the shading event (uv, point, normal, noise, Fresnel input)? */
+bool GraphCompiler::context_free(int off, int len) const {
+    for (int i = 0; i < len; ++i) {
+        const uint8_t op = (*code)[off + i].op;
+        if (op == OP_UV || op == OP_POINT || op == OP_NORMAL || op == OP_NOISE || op == OP_SCHLICK) return false;
+    }
+    return true;
+}
+
+/* RGB mode: evaluate a context-free material program once, here. */
+void GraphCompiler::fold_material(DMaterial &m) {
+    m.folded = 0;
+    if (!context_free(m.prog_off, m.prog_len)) return;
+    float4 R[LGPU_MAX_REGS];
+    std::memset(R, 0, sizeof(R));
+    ShadeCtx ctx;
+    std::memset(&ctx, 0, sizeof(ctx));
+    ctx.eta = 1.001f;
+    Lambda4 lam;
+    std::memset(&lam, 0, sizeof(lam));
+    run_prog<3>(code->data() + m.prog_off, m.prog_len, ctx, lam, R);
+    for (int i = 0; i < m.num_leaves; ++i) { m.kalb[i] = R[m.leaves[i].albedo]; m.kalb[i].w = 0.f; m.krough[i] = R[m.leaves[i].rough].x; }
+    for (int i = 0; i < m.num_tree; ++i) m.kratio[i] = m.tree[i].kind ? R[m.tree[i].ratio].x : 0.f;
+    m.folded = 1;
 }
 
 bool GraphCompiler::compile_emission(int node, int socket, int &prog_off, int &prog_len, int &out_reg) {
@@ -537,6 +564,22 @@ bool GraphCompiler::compile_emission(int node, int socket, int &prog_off, int &p
     code->push_back(c1);
     code->push_back(c2);
     prog_len = (int)code->size() - prog_off;
+    return true;
+}
+
+/* RGB mode: evaluate a context-free emission program once; returns false if it reads the event. */
+bool GraphCompiler::fold_emission(int prog_off, int prog_len, int out_reg, float4 em[2]) {
+    if (!context_free(prog_off, prog_len)) return false;
+    float4 R[LGPU_MAX_REGS];
+    std::memset(R, 0, sizeof(R));
+    ShadeCtx ctx;
+    std::memset(&ctx, 0, sizeof(ctx));
+    ctx.eta = 1.001f;
+    Lambda4 lam;
+    std::memset(&lam, 0, sizeof(lam));
+    run_prog<3>(code->data() + prog_off, prog_len, ctx, lam, R);
+    em[0] = R[out_reg]; em[0].w = 0.f;
+    em[1] = R[out_reg + 1]; em[1].w = 0.f;
     return true;
 }
 

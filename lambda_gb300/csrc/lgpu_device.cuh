@@ -741,10 +741,22 @@ __device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
 __device__ __forceinline__ int4 ldg4i(const int4 *p) { return __ldg(p); }
 #endif
 
+/* Traversal stacks: per-thread local array, or a column of a shared-memory block array
+ * (entry i of thread t at i * LG_SMEM_STRIDE + t: every lane hits its own bank). */
+struct LocalStack {
+    int v[LGPU_STACK];
+    __device__ __forceinline__ int &operator[](int i) { return v[i]; }
+};
+#define LG_SMEM_STRIDE 128
+struct SmemStack {
+    int *p;
+    __device__ __forceinline__ int &operator[](int i) { return p[i * LG_SMEM_STRIDE]; }
+};
+
 /* Closest hit (any_hit = false) or occlusion (any_hit = true) over TLAS + BLAS. */
-template <bool COUNT>
-__device__ __noinline__ bool traverse(const DeviceScene &S, float3 wo, float3 wd, float tmax, bool any_hit, HitRec *hr, TravStats *st) {
-    int stack[LGPU_STACK];
+template <bool COUNT, class STK>
+__device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, float3 wd, float tmax, bool any_hit, HitRec *hr,
+                                           TravStats *st, STK &stack) {
     int sp = 0;
     stack[sp++] = S.root;   /* encoded child ref of the root */
     float3 o = wo, d = wd;
@@ -815,6 +827,12 @@ __device__ __noinline__ bool traverse(const DeviceScene &S, float3 wo, float3 wd
         if (sp >= LGPU_STACK - 2) sp = LGPU_STACK - 2;   /* never reached for BVH depths < 60 */
     }
     return hit;
+}
+
+template <bool COUNT>
+__device__ __noinline__ bool traverse(const DeviceScene &S, float3 wo, float3 wd, float tmax, bool any_hit, HitRec *hr, TravStats *st) {
+    LocalStack stk;
+    return traverse_t<COUNT>(S, wo, wd, tmax, any_hit, hr, st, stk);
 }
 
 /* Object::Hit + TriangleMesh/Instance::ProcessHit (Object.h:27-35, TriangleMesh.cpp:80-114,

@@ -14,7 +14,7 @@ namespace lg {
  * reference (`nl != l`). */
 struct LRef { int light, tri; };
 
-#define LG_MAX_TREE_DEPTH 48
+#define LG_MAX_TREE_DEPTH 64
 HD bool lref_eq(LRef a, LRef b) { return a.light == b.light && a.tri == b.tri; }
 
 template <int NS, bool COUNT>
@@ -85,6 +85,7 @@ struct Tracer {
 
     /* ---------------------------------------------------------------- emission programs */
     __device__ __noinline__ Spec<NS> emission(const DLight &L, const Event &ev, const RayHit &h, bool illum) {
+        if (NS == 3 && L.em_folded) return Spec<NS>::from4(illum ? L.em[0] : L.em[1]);
         float4 R[LGPU_MAX_REGS];
         ShadeCtx c;
         c.point = h.point; c.normalS = h.nS; c.uv = h.uv; c.woLy = ev.woL.y; c.eta = ev.eta;
@@ -334,22 +335,38 @@ struct Tracer {
     }
 
     /* ---------------------------------------------------------------- light samplers */
-    /* ManyLightSampler::ImportanceMeasure (ManyLightSampler.cpp:305-326) */
+    /* ManyLightSampler::ImportanceMeasure (ManyLightSampler.cpp:305-326), useSplits = true:
+     *   theta  = acos(delta . axis), thetaU = atan(r / d), thetaDash = max(theta - thetaO - thetaU, 0)
+     *   I = cos(max(thetaI - thetaU, 0)) * E / d^2 * cos(thetaDash)   if thetaDash < thetaE (= pi/2)
+     * evaluated with cosine/sine identities instead of acos / atan / cos (same value to ~1e-6
+     * relative).  The reference's NaN cases are kept: a cone cosine outside [-1, 1] gives 0, a normal
+     * cosine outside [-1, 1] gives NaN. */
     __device__ __forceinline__ float importance(float3 p, float3 nS, const DLNode &n) {
         float3 delta = n.center - p;
-        const float diam = n.diag;
         const float d2 = dot(delta, delta);
         const float dd = sqrtf(d2);
         const float invD = 1.f / dd;
         delta = delta * invD;
-        const float theta = acosf(dot(delta, n.axis));
-        const float thetaU = atanf((diam * .5f) * invD);
-        const float thetaD = smax(theta - n.thetaO - thetaU, 0.f);
-        if (thetaD < n.thetaE) {
-            const float thetaI = acosf(dot(delta, nS));
-            return (cosf(smax(thetaI - thetaU, 0.f)) * n.power) / d2 * cosf(thetaD);
+        const float cosT = dot(delta, n.axis);
+        if (!(cosT >= -1.f && cosT <= 1.f)) return 0.f;
+        const float tU = (n.diag * .5f) * invD;
+        const float cosU = 1.f / sqrtf(1.f + tU * tU), sinU = tU * cosU;
+        const float cosA = n.cosO * cosU - n.sinO * sinU;   /* a = thetaO + thetaU */
+        const float sinA = n.sinO * cosU + n.cosO * sinU;
+        float cosDash = 1.f;
+        if (!(sinA < 0.f || cosT >= cosA)) {               /* theta > a (and a <= pi) */
+            const float sinT = sqrtf(smax(0.f, 1.f - cosT * cosT));
+            cosDash = cosT * cosA + sinT * sinA;
+            if (!(cosDash > 0.f)) return 0.f;               /* thetaDash >= thetaE = pi/2 */
         }
-        return 0.f;
+        const float cosI = dot(delta, nS);
+        if (!(cosI >= -1.f && cosI <= 1.f)) return __int_as_float(0x7fc00000);
+        float cosTerm = 1.f;
+        if (cosI < cosU) {                                  /* thetaI > thetaU */
+            const float sinI = sqrtf(smax(0.f, 1.f - cosI * cosI));
+            cosTerm = cosI * cosU + sinI * sinU;
+        }
+        return (cosTerm * n.power) / d2 * cosDash;
     }
     __device__ LRef tree_light_ref(int idx) {
         const int2 tl = __ldg(&S.tree_lights[idx]);
@@ -409,25 +426,20 @@ struct Tracer {
         const int2 slot = __ldg(&S.tree_slot[ti]);
         const DLNode &leaf = S.lnodes[slot.x];
         const float pdf = S.fpool[leaf.dist_off + leaf.num + 1 + slot.y];   /* raw power (Piecewise1D::PDF) */
-        /* the reference multiplies the branch probabilities from the root down (recursion) */
-        float lev[LG_MAX_TREE_DEPTH];
-        int depth = 0;
+        /* branch probabilities multiplied leaf-up (the reference's recursion multiplies root-down;
+         * the two orders agree to a few ulps) */
         int child = slot.x;
         int ni = leaf.parent;
-        while (ni >= 0 && depth < LG_MAX_TREE_DEPTH) {
+        float acc = 1.f;
+        for (int depth = 0; ni >= 0 && depth < LG_MAX_TREE_DEPTH; ++depth) {
             const DLNode &n = S.lnodes[ni];
             const DLNode cl = S.lnodes[n.child0], cr = S.lnodes[n.child0 + 1];
             const float IL = importance(p, nS, cl);
             const float IR = importance(p, nS, cr);
             const float p0 = IL / (IL + IR);
-            lev[depth++] = (child == n.child0) ? p0 : 1.f - p0;
+            acc = ((child == n.child0) ? p0 : 1.f - p0) * acc;
             child = ni;
             ni = n.parent;
-        }
-        float acc = 1.f;
-        if (depth > 0) {
-            acc = lev[depth - 1];
-            for (int k = depth - 2; k >= 0; --k) acc = lev[k] * acc;
         }
         return pdf * acc;
     }
@@ -435,6 +447,11 @@ struct Tracer {
     /* ---------------------------------------------------------------- BSDF setup */
     __device__ __noinline__ void setup_bsdf(Bsdf<NS> &b, const DMaterial &m, const Event &ev, const RayHit &h) {
         b.m = &m;
+        if (NS == 3 && m.folded) {   /* context-free graph evaluated at scene compile */
+            for (int i = 0; i < m.num_leaves; ++i) { b.alb[i] = Spec<NS>::from4(m.kalb[i]); b.rough[i] = m.krough[i]; }
+            for (int i = 0; i < m.num_tree; ++i) b.ratio[i] = m.kratio[i];
+            return;
+        }
         float4 R[LGPU_MAX_REGS];
         ShadeCtx c;
         c.point = h.point; c.normalS = h.nS; c.uv = h.uv; c.woLy = ev.woL.y; c.eta = ev.eta;

@@ -258,9 +258,10 @@ void build_light_tree(const std::vector<TreeLightIn> &lights, std::vector<float>
         d.center = make_float3(c.x, c.y, c.z);
         d.diag = n.b.diagonal();
         d.axis = make_float3(n.cone.axis.x, n.cone.axis.y, n.cone.axis.z);
-        d.thetaO = n.cone.thetaO;
-        d.thetaE = n.cone.thetaE;
+        d.cosO = std::cos(n.cone.thetaO);
+        d.sinO = std::sin(n.cone.thetaO);
         d.power = n.power;
+        if (n.cone.thetaE != PIf / 2.f) { out.root = -2; return; }   /* invariant of the reference's cones */
         d.child0 = n.ch[0] >= 0 ? n.ch[0] + 1 : -1;
         d.parent = n.parent >= 0 ? n.parent + 1 : -1;
         d.first = (int)n.first;

@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(128) k_wave_resume(WaveArgs W, int n) {
         int seg = 0;
 #pragma unroll
         for (int k = 1; k < LG_NSEG; ++k) seg += (i >= W.seg_off[k]) ? 1 : 0;
-        slot = W.queue_in[seg * W.cap + (i - W.seg_off[seg])];
+        slot = W.queue_in[seg * W.cap_in + (i - W.seg_off[seg])];
     }
     PHot<NS> *G = reinterpret_cast<PHot<NS> *>(W.states);
     PHot<NS> *sh = reinterpret_cast<PHot<NS> *>(smem4) + (threadIdx.x & ~31);
@@ -271,22 +271,23 @@ size_t LG_CAT(wave_cold_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PCold<LGP
 #if LGPU_NS == 3
 /* Answer every queued query: closest hit (Scene::Intersect) or occlusion (rtcOccluded1). */
 template <bool COUNT>
-__global__ void __launch_bounds__(256) k_wave_trace(WaveArgs W, int n) {
+__global__ void __launch_bounds__(128) k_wave_trace(WaveArgs W, int n) {
+    LocalStack stk;   /* measured faster than a shared-memory column stack (L1 serves it) */
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     TravStats st = {0u, 0u, 0u};
     if (i < n) {
         int seg = 0;
 #pragma unroll
         for (int k = 1; k < LG_NSEG; ++k) seg += (i >= W.seg_off[k]) ? 1 : 0;
-        const int slot = W.queue_in[seg * W.cap + (i - W.seg_off[seg])];
+        const int slot = W.queue_in[seg * W.cap_in + (i - W.seg_off[seg])];
         const float4 o = W.qo[slot], d = W.qd[slot];
         HitRec hr;
         if (__float_as_int(d.w) == Q_CLOSEST) {
-            const bool ok = traverse<COUNT>(W.S, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), finf(), false, &hr, &st);
+            const bool ok = traverse_t<COUNT>(W.S, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), finf(), false, &hr, &st, stk);
             W.res[slot] = ok ? make_float4(hr.t, hr.u, hr.v, __int_as_float(hr.prim)) : make_float4(finf(), 0.f, 0.f, 0.f);
             W.res_obj[slot] = ok ? hr.obj : -1;
         } else {
-            const bool occ = traverse<COUNT>(W.S, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), o.w, true, &hr, &st);
+            const bool occ = traverse_t<COUNT>(W.S, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), o.w, true, &hr, &st, stk);
             W.res[slot] = make_float4(occ ? 1.f : 0.f, 0.f, 0.f, 0.f);
         }
     }
@@ -303,7 +304,8 @@ __global__ void __launch_bounds__(256) k_wave_trace(WaveArgs W, int n) {
 }
 cudaError_t LG_CAT(wave_trace_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_wave_trace<LGPU_COUNT != 0><<<(n + 255) / 256, 256, 0, st>>>(W, n);
+    const int bs = 128;
+    k_wave_trace<LGPU_COUNT != 0><<<(n + bs - 1) / bs, bs, 0, st>>>(W, n);
     return cudaGetLastError();
 }
 #endif

@@ -85,6 +85,10 @@ struct DMaterial {
     int num_leaves, num_tree;
     DLeaf leaves[LGPU_MAX_LEAVES];
     DBsdfNode tree[2 * LGPU_MAX_LEAVES - 1];
+    int folded;                  /* RGB mode: graph is context-free, constants below are its values */
+    float4 kalb[LGPU_MAX_LEAVES];
+    float krough[LGPU_MAX_LEAVES];
+    float kratio[2 * LGPU_MAX_LEAVES - 1];
 };
 
 enum { LT_POINT = 0, LT_MESH = 1, LT_ENV = 2, LT_SPOT = 3, LT_TRI = 4 };
@@ -102,7 +106,8 @@ struct DLight {
     float3 pos;
     float3 axis;
     float power;
-    float pad;
+    int em_folded;                     /* RGB mode: emission graph is context-free */
+    float4 em[2];                      /* its illuminant and reflectance spectra */
 };
 
 /* Flattened ManyLightSampler node (ManyLightSampler.h:47-60), 64 bytes.  Bounds are stored as the
@@ -114,8 +119,8 @@ struct __align__(16) DLNode {
     float3 center;
     float diag;
     float3 axis;
-    float thetaO;
-    float thetaE, power;
+    float cosO;          /* cos / sin of the orientation-cone angle thetaO; every node's emission */
+    float sinO, power;   /* angle thetaE is pi/2 (MakeCone's default, kept by OrientationCone::Union) */
     int child0, parent;
     int first, num;      /* light range in tree order */
     int dist_off;        /* leaf: CDF (num+1) then raw powers (num) in fpool */

@@ -107,7 +107,8 @@ struct WaveArgs {
     int *queue_out;
     int *count_out;               /* LG_NSEG counters of queue_out */
     int seg_off[LG_NSEG + 1];     /* prefix offsets of the queue_in segments */
-    int cap;
+    int cap;                      /* capacity of one queue_out segment */
+    int cap_in;                   /* stride between queue_in segments */
     int *free_list;               /* slots whose path ended this iteration */
     int *free_count;
     unsigned long long *next_path;
