@@ -295,6 +295,11 @@ LGPU_API const char *lgpu_last_error(const lgpu_context *ctx);
  * LightSampler::Commit (ManyLightSampler.cpp:37-44). */
 LGPU_API int lgpu_scene_commit(lgpu_context *ctx, const lgpu_scene_desc *scene);
 
+/* Compile and validate a scene on the host only, without a GPU or a context (the host half of
+ * lgpu_scene_commit).  Writes a one-line report (counts, or the first error) into `report`
+ * (NUL-terminated, truncated to report_size).  Returns the status lgpu_scene_commit would. */
+LGPU_API int lgpu_scene_check(const lgpu_scene_desc *scene, char *report, size_t report_size);
+
 /* Render `opts->spp` samples per pixel and ADD them to the host film `film_rgbn`
  * (width*height float4: summed RGB + sample count), the way Film::AddSample accumulates
  * (src/camera/Film.h:30-33).  Host buffers: the call copies the film to and from the device.
