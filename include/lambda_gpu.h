@@ -332,6 +332,37 @@ LGPU_API int lgpu_render_count(lgpu_context *ctx, const lgpu_camera_desc *camera
 LGPU_API int lgpu_intersect(lgpu_context *ctx, const float *rays_dev, uint32_t *hits_dev,
                             float *uv_out_dev, uint64_t n, void *stream);
 
+/* Fixed-scratch variant of lgpu_render_paths, for callers that must not allocate.
+ * No counterpart in the reference, which renders on the CPU.
+ *
+ * Who needs it: a host that drives the renderer from a region where allocating device memory is
+ * not allowed or not affordable, e.g. a caller whose device memory is fully handed to another
+ * allocator (a framework's caching pool), or a frame loop that cannot take the implicit
+ * device-wide synchronisation of cudaMalloc / cudaFree.  lgpu_render_paths grows buffers inside
+ * the context on demand; this entry point never does.
+ *
+ * Same paths, same random-number order and the same per-path result as lgpu_render_paths, but:
+ *   - path_ids_dev (n ids, uint64) and path_out_dev (n x 4 floats: radiance, random numbers
+ *     drawn) are DEVICE buffers owned by the caller; ids must be < width * height * spp (larger
+ *     ids are not detected and give unspecified values, no out-of-bounds access);
+ *   - the working memory is one array of at most LGPU_NOALLOC_SCRATCH_BYTES compiled into the
+ *     library (one copy per device), holding a pool of at most LGPU_NOALLOC_MAX_SLOTS paths in
+ *     flight; any n streams through that pool.  opts->pool_slots = 0 uses the whole pool, values
+ *     above LGPU_NOALLOC_MAX_SLOTS are rejected with LGPU_ERR_INVALID_ARG;
+ *   - the wavefront kernels always run (kernel_mode MEGAKERNEL is rejected); no traversal counters.
+ * The call issues its work on `stream` and returns when it has finished.  The first call on a
+ * device also looks up the array's address (cudaGetSymbolAddress) and may make the driver load
+ * the kernels' code, so make it before any stream capture or allocation-free region starts.
+ * The scratch and its counters (which must start at zero) are cleared by the call itself.
+ * The array is shared by every context on a device: overlapping calls would race on it, so calls
+ * on one device are serialised by a lock inside the library; do not issue them from code that
+ * cannot block.  Error paths store their message in the context (host memory). */
+#define LGPU_NOALLOC_MAX_SLOTS 16384
+#define LGPU_NOALLOC_SCRATCH_BYTES (16u << 20)
+LGPU_API int lgpu_render_paths_noalloc(lgpu_context *ctx, const lgpu_camera_desc *camera,
+                                       const lgpu_render_opts *opts, const uint64_t *path_ids_dev,
+                                       uint64_t n, float *path_out_dev, void *stream);
+
 LGPU_API int lgpu_get_stats(const lgpu_context *ctx, lgpu_stats *out);
 
 /* Version string of the module. */

@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1173,6 +1174,156 @@ LGPU_API int lgpu_intersect(lgpu_context *c, const float *rays_dev, uint32_t *hi
     if (e != cudaSuccess) return cuda_fail(c, e, "intersect launch");
     e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "intersect");
+    return LGPU_OK;
+}
+
+}  // extern "C"
+
+/* ------------------------------------------------------------------ fixed-scratch path render
+ *
+ * lgpu_render_paths_noalloc runs the same wavefront kernels as lgpu_render_paths, but its whole
+ * working set (path-state pool, ray/hit records, stage queues, free list, counters) is carved out
+ * of one device array with static storage in this file, and the ids and results live in buffers
+ * the caller already owns.  Once the array's address is known the call makes no allocation,
+ * device or host: it only issues memsets, kernel launches and small device-to-host reads of the
+ * queue counts into a stack array.
+ *
+ * Layout of the array (each region starts on a 256-byte boundary), for S = LGPU_NOALLOC_MAX_SLOTS:
+ *   hot path state   S x max(sizeof PHot<3>, PHot<4>)
+ *   cold path state  S x max(sizeof PCold<3>, PCold<4>)
+ *   ray origin, ray direction, hit record   3 x S x 16 B
+ *   hit object, free list                   2 x S x 4 B
+ *   stage queues A and B                    2 x LG_NSEG x S x 4 B
+ *   queue counts, free count                (2 x LG_NSEG + 2) x 4 B
+ *   next-path counter                       8 B
+ * Only the counts and the next-path counter must be zero when a call starts; the call clears them
+ * itself on the caller's stream.  Everything else is written before it is read. */
+namespace {
+
+constexpr size_t na_round(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr size_t na_max(size_t a, size_t b) { return a > b ? a : b; }
+constexpr size_t NA_SLOTS = LGPU_NOALLOC_MAX_SLOTS;
+constexpr size_t NA_HOT = na_max(sizeof(PHot<3>), sizeof(PHot<4>));
+constexpr size_t NA_COLD = na_max(sizeof(PCold<3>), sizeof(PCold<4>));
+constexpr size_t NA_OFF_COLD = na_round(NA_HOT * NA_SLOTS);
+constexpr size_t NA_OFF_QO = NA_OFF_COLD + na_round(NA_COLD * NA_SLOTS);
+constexpr size_t NA_OFF_QD = NA_OFF_QO + na_round(16 * NA_SLOTS);
+constexpr size_t NA_OFF_RES = NA_OFF_QD + na_round(16 * NA_SLOTS);
+constexpr size_t NA_OFF_RESOBJ = NA_OFF_RES + na_round(16 * NA_SLOTS);
+constexpr size_t NA_OFF_FREE = NA_OFF_RESOBJ + na_round(4 * NA_SLOTS);
+constexpr size_t NA_OFF_QA = NA_OFF_FREE + na_round(4 * NA_SLOTS);
+constexpr size_t NA_OFF_QB = NA_OFF_QA + na_round(4 * LG_NSEG * NA_SLOTS);
+constexpr size_t NA_OFF_COUNTS = NA_OFF_QB + na_round(4 * LG_NSEG * NA_SLOTS);
+constexpr size_t NA_OFF_NEXT = NA_OFF_COUNTS + na_round(4 * (2 * LG_NSEG + 2));
+constexpr size_t NA_BYTES = NA_OFF_NEXT + na_round(8);
+static_assert(NA_BYTES <= LGPU_NOALLOC_SCRATCH_BYTES, "fixed scratch larger than its stated bound");
+
+__device__ __align__(256) static unsigned char g_na_scratch[NA_BYTES];
+
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mutex[NA_MAX_DEVICES];
+unsigned char *g_na_base[NA_MAX_DEVICES] = {};
+
+}  // namespace
+
+extern "C" {
+
+LGPU_API int lgpu_render_paths_noalloc(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o,
+                                       const uint64_t *path_ids_dev, uint64_t n, float *path_out_dev, void *stream) {
+    int r = check_opts(c, cam, o);
+    if (r) return r;
+    if (n == 0) return LGPU_OK;
+    if (!path_ids_dev || !path_out_dev) return fail(c, LGPU_ERR_INVALID_ARG, "null path buffers");
+    if (o->kernel_mode == LGPU_KERNEL_MEGAKERNEL)
+        return fail(c, LGPU_ERR_INVALID_ARG, "lgpu_render_paths_noalloc runs the wavefront kernels only");
+    if (o->pool_slots < 0 || o->pool_slots > LGPU_NOALLOC_MAX_SLOTS) {
+        char msg[160];
+        std::snprintf(msg, sizeof(msg), "pool_slots %d is outside the fixed scratch pool (1..%d slots, 0 = all)",
+                      o->pool_slots, LGPU_NOALLOC_MAX_SLOTS);
+        return fail(c, LGPU_ERR_INVALID_ARG, msg);
+    }
+    if (c->device < 0 || c->device >= NA_MAX_DEVICES) return fail(c, LGPU_ERR_INVALID_ARG, "device ordinal out of range");
+    const bool hero = o->spectral_mode == LGPU_SPECTRAL_HERO4;
+    if ((hero ? wave_state_bytes_4_0() : wave_state_bytes_3_0()) > NA_HOT ||
+        (hero ? wave_cold_bytes_4_0() : wave_cold_bytes_3_0()) > NA_COLD)
+        return fail(c, LGPU_ERR_INVALID_ARG, "path-state layout larger than the fixed scratch slots");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(c, e, "set device");
+    std::lock_guard<std::mutex> lock(g_na_mutex[c->device]);
+    if (!g_na_base[c->device]) {   /* once per device: the address of this device's copy */
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_na_scratch);
+        if (e != cudaSuccess) return cuda_fail(c, e, "scratch symbol address");
+        g_na_base[c->device] = static_cast<unsigned char *>(p);
+    }
+    unsigned char *base = g_na_base[c->device];
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t slots = (size_t)std::min<uint64_t>(n, o->pool_slots > 0 ? (uint64_t)o->pool_slots : NA_SLOTS);
+
+    WaveArgs W;
+    std::memset(&W, 0, sizeof(W));
+    W.S = c->S;
+    W.cam = make_cam(cam, o);
+    W.rp.spp = o->spp; W.rp.max_bounces = o->max_bounces; W.rp.min_bounces = o->min_bounces;
+    W.rp.seed = o->seed; W.rp.sample_offset = o->sample_offset;
+    W.states = base;
+    W.cold = base + NA_OFF_COLD;
+    W.qo = reinterpret_cast<float4 *>(base + NA_OFF_QO);
+    W.qd = reinterpret_cast<float4 *>(base + NA_OFF_QD);
+    W.res = reinterpret_cast<float4 *>(base + NA_OFF_RES);
+    W.res_obj = reinterpret_cast<int *>(base + NA_OFF_RESOBJ);
+    W.free_list = reinterpret_cast<int *>(base + NA_OFF_FREE);
+    W.next_path = reinterpret_cast<unsigned long long *>(base + NA_OFF_NEXT);
+    W.n_paths = n;
+    W.base = 0;
+    W.ids = path_ids_dev;
+    W.path_out = reinterpret_cast<float4 *>(path_out_dev);
+    W.counters = c->d_counters;
+    W.cap = (int)slots;
+    W.cap_in = (int)slots;
+    int *counts = reinterpret_cast<int *>(base + NA_OFF_COUNTS);
+    int *qa = reinterpret_cast<int *>(base + NA_OFF_QA), *qb = reinterpret_cast<int *>(base + NA_OFF_QB);
+    int *ca = counts, *cb = counts + LG_NSEG;
+    W.free_count = counts + 2 * LG_NSEG;
+    auto resume = [&](int m, int mode) { return hero ? wave_resume_4_0(W, m, mode, st) : wave_resume_3_0(W, m, mode, st); };
+
+    e = cudaMemsetAsync(counts, 0, (2 * LG_NSEG + 2) * sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(W.next_path, 0, sizeof(unsigned long long), st);
+    W.queue_in = nullptr; W.queue_out = qa; W.count_out = ca;
+    if (e == cudaSuccess) e = resume((int)slots, 2);   /* fill the pool */
+    if (e != cudaSuccess) return cuda_fail(c, e, "wavefront start");
+    int h_count[LG_NSEG];
+    int iters = 0;
+    for (;;) {
+        e = cudaMemcpyAsync(h_count, ca, sizeof(h_count), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "wavefront");
+        int m = 0;
+        W.seg_off[0] = 0;
+        for (int k = 0; k < LG_NSEG; ++k) { m += h_count[k]; W.seg_off[k + 1] = m; }
+        if (m <= 0) break;
+        if (++iters > 100000) return fail(c, LGPU_ERR_TIMEOUT, "wavefront did not drain");
+        e = cudaMemsetAsync(cb, 0, LG_NSEG * sizeof(int), st);
+        W.queue_in = qa; W.queue_out = qb; W.count_out = cb;
+        if (e == cudaSuccess) e = wave_trace_3_0(W, m, st);
+        const WaveArgs W0 = W;
+        for (int k = 0; k < LG_NSEG && e == cudaSuccess; ++k) {   /* one resume launch per stage */
+            const int nk = W0.seg_off[k + 1] - W0.seg_off[k];
+            if (nk <= 0) continue;
+            for (int j = 0; j <= LG_NSEG; ++j) W.seg_off[j] = j <= k ? 0 : 0x7fffffff;
+            W.queue_in = qa + (size_t)k * W0.cap;
+            W.cap_in = 0;
+            e = resume(nk, 0);
+            W = W0;
+        }
+        if (e == cudaSuccess) e = resume(m, 1);   /* new paths into the freed slots */
+        if (e != cudaSuccess) return cuda_fail(c, e, "wavefront iteration");
+        std::swap(qa, qb);
+        std::swap(ca, cb);
+    }
+    c->stats.paths = n;
+    c->stats.iterations = (uint32_t)iters;
+    c->stats.pool_slots = (uint32_t)slots;
     return LGPU_OK;
 }
 
