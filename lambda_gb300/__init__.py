@@ -29,7 +29,7 @@ class LambdaGPUError(RuntimeError):
 
 
 def build(force=False):
-    from .build import build as _b
+    from .build_ext import build as _b
     return _b(force=force)
 
 
@@ -136,4 +136,8 @@ class Renderer:
     def stats(self):
         s = abi.Stats()
         self._check(lib().lgpu_get_stats(self._h, C.byref(s)))
-        return {f: getattr(s, f) for f, _ in abi.Stats._fields_}
+        out = {}
+        for f, _ in abi.Stats._fields_:
+            v = getattr(s, f)
+            out[f] = list(v) if hasattr(v, "__len__") else v
+        return out
