@@ -7,8 +7,11 @@ is additionally flushed between timed steps.
 
   value   device-resident throughput: K frames launched back to back on one stream, CUDA events
   e2e     the same metric through lgpu_render with a host film (H2D + D2H film copies inside)
-  roofline  algorithmic BVH bytes (node + triangle records fetched, counted in-kernel by a separate
-          counting launch of the same frame) / kernel time, against the measured HBM copy peak
+  roofline  for the kernel with the largest share of the frame: its algorithmic bytes (resume: path
+          state in and out per resumed path; trace: BVH node and triangle records fetched, counted
+          in-kernel by a separate counting render of the same frame, plus ray and hit records) over
+          its own time, taken from CUDA events the library records around every launch on the render
+          stream; all kernels are listed under roofline.kernels
   cpu_baseline  the CPU oracle (restatement of the reference integrator) on this host's cores over
           a bounded stratified sample of the same frame
 
@@ -35,9 +38,15 @@ UNIT = "Mpath-samples/s"
 WORKLOAD = dict(workload="many-light terrain (2.1M tris, 10k emitters, sky env), MIS volumetric path tracing",
                 width=1920, height=1080, spp=64, max_depth=6, triangles=2093058 + 10000, emitters=10000,
                 spectral="RGB3", light_sampler="light tree")
-# DRAM bytes per launch of the render kernel from one ncu capture (profiles/render_terrain_1080p.md),
-# scaled to the full frame; None until captured.
-NCU_TRAFFIC_PER_LAUNCH = None
+# DRAM bytes (read + write) per unit of work of each wavefront kernel, from one ncu capture of a
+# smaller frame of the same scene (profiles/wavefront_terrain.md); multiplied by the units of an
+# average launch of the timed run.  None until captured.
+NCU_DRAM_BYTES_PER_UNIT = {"k_wave_resume": None, "k_wave_trace": None}
+# Algorithmic bytes per unit: a resumed path reads and writes its path state (96 B each way: ray,
+# throughput, radiance, pdfs, medium, depth, ids); a traced ray fetches its BVH nodes and triangle
+# records (counted in-kernel) plus 32 B of ray and 20 B of hit record.
+STATE_BYTES_PER_RESUME = 192
+RAY_IO_BYTES = 52
 
 
 def parse():
@@ -128,7 +137,7 @@ def cpu_baseline(sb, cam, opts, seconds, threads=0):
         px = (np.arange(npix, dtype=np.uint64) * step + offset) % (W * H)
         return (px[:, None] * spp + np.arange(spp, dtype=np.uint64)[None, :]).reshape(-1)
 
-    calib = ids_for(max(1, 512 // spp * 8), 7)
+    calib = ids_for(max(1, 2048 // spp * 8), 7)
     t0 = time.perf_counter()
     o.render_paths(cam, opts, calib, threads=threads)
     dt = time.perf_counter() - t0
@@ -142,6 +151,54 @@ def cpu_baseline(sb, cam, opts, seconds, threads=0):
     return {"value": len(ids) / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%d of %d pixels (stratified, every %dth) x %d spp = %d path samples in %.1f s"
                       % (npix, W * H, max(1, (W * H) // npix), spp, len(ids), dt)}
+
+
+def replica_seed(rank):
+    """Replicas: every rank renders its own frame of the same scene with its own seed."""
+    return 1 + rank
+
+
+def max_over_ranks(values, dist, device):
+    """Element-wise max over ranks of per-rank timings (the job takes as long as its slowest rank)."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def job_throughput(paths_per_rank, steps, world, ms):
+    """Whole-job Mpath-samples/s: the paths all ranks rendered over the slowest rank's time."""
+    return paths_per_rank * steps * world / (ms / 1e3) / 1e6
+
+
+def kernel_table(per_step, stats, paths, kernel_ms, megakernel):
+    """Per-kernel time, work units and algorithmic bytes of one frame (mean over timed frames)."""
+    trav_bytes = stats["nodes_visited"] * stats["node_bytes"] + stats["tris_tested"] * stats["tri_record_bytes"] \
+        + stats["rays"] * RAY_IO_BYTES
+    mean = lambda f: float(np.mean([f(s_) for s_ in per_step]))
+    k = {}
+    if megakernel:
+        k["k_render"] = {"ms": float(np.mean(kernel_ms)), "launches": 1.0, "units": float(paths),
+                         "alg_bytes": float(trav_bytes + paths * 16)}
+    else:
+        iters = mean(lambda s_: s_["iterations"])
+        resumed = mean(lambda s_: sum(s_["resumed"]))
+        # launches per frame: first spawn 2, per iteration trace 1 + spawn 2 + one resume per
+        # non-empty stage, film reduction 1
+        k["k_wave_resume"] = {"ms": mean(lambda s_: s_["shade_ms"]),
+                              "launches": mean(lambda s_: s_["launches"]) - 3 * iters - 3, "units": resumed,
+                              "alg_bytes": resumed * STATE_BYTES_PER_RESUME,
+                              "stage_ms": [mean(lambda s_: s_["stage_ms"][j]) for j in range(6)],
+                              "stage_paths": [mean(lambda s_: s_["resumed"][j]) for j in range(6)]}
+        k["k_wave_trace"] = {"ms": mean(lambda s_: s_["trace_ms"]), "launches": iters,
+                             "units": mean(lambda s_: s_["traced"]), "alg_bytes": float(trav_bytes)}
+        k["k_wave_spawn"] = {"ms": mean(lambda s_: s_["spawn_ms"]), "launches": iters + 1, "units": float(paths),
+                             "alg_bytes": float(paths * (STATE_BYTES_PER_RESUME // 2 + 32))}
+    for k_ in k.values():
+        k_["achieved_gbs"] = k_["alg_bytes"] / (k_["ms"] / 1e3) / 1e9 if k_["ms"] > 0 else None
+    return k
 
 
 def main():
@@ -183,7 +240,7 @@ def main():
     dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
     sb, cam, opts = configs.terrain(args.width, args.height, args.spp, 6)
-    opts.seed = 1 + rank
+    opts.seed = replica_seed(rank)
     opts.kernel_mode = {"auto": abi.KERNEL_AUTO, "megakernel": abi.KERNEL_MEGAKERNEL, "wavefront": abi.KERNEL_WAVEFRONT}[args.mode]
     opts.pool_slots = args.pool
     r = lg.Renderer(sb, device=dev)
@@ -194,12 +251,6 @@ def main():
     stream = torch.cuda.current_stream().cuda_stream
     # counting launch (outside the timed region): nodes / triangles / rays of one frame
     stats = r.render_count(cam, opts)
-    breakdown = None
-    if os.environ.get("LGPU_PROFILE"):
-        r.render_device(cam, opts, film.data_ptr(), stream=stream)
-        torch.cuda.synchronize()
-        b = r.stats()
-        breakdown = {k: b[k] for k in ("trace_ms", "shade_ms", "spawn_ms", "iterations", "pool_slots")}
     for _ in range(args.warmup):
         r.render_device(cam, opts, film.data_ptr(), stream=stream)
     torch.cuda.synchronize()
@@ -211,18 +262,20 @@ def main():
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
+    per_step = []
     t_start.record()
     for k in range(args.steps):
         flush.zero_()
         ev[k][0].record()
         r.render_device(cam, opts, film.data_ptr(), stream=stream)
         ev[k][1].record()
+        per_step.append(r.stats())   # host-side copy of the library's per-launch event timings
     t_end.record()
     torch.cuda.synchronize()
     total_ms = t_start.elapsed_time(t_end)
     kernel_ms = [a.elapsed_time(b) for a, b in ev]
     # every path of every rendered frame must have reached the film (no work skipped)
-    rendered = args.warmup + args.steps + (1 if os.environ.get("LGPU_PROFILE") else 0)
+    rendered = args.warmup + args.steps
     counts = film[..., 3]
     if not bool(torch.all(counts == float(spp * rendered))):
         raise SystemExit("work check failed: film sample counts %s, expected %d per pixel"
@@ -236,35 +289,32 @@ def main():
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     clk = clocks.stop()
+    total_ms, e2e_ms = max_over_ranks([total_ms, e2e_s * 1e3], dist, "cuda")
     if dist:
-        t = torch.tensor([total_ms, e2e_s * 1e3], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_ms = float(t[0]), float(t[1])
         dist.barrier()
-    else:
-        e2e_ms = e2e_s * 1e3
-    value = paths * args.steps * world / (total_ms / 1e3) / 1e6
-    st_now = r.stats()
-    # kernels of ours per timed step: megakernel 1; wavefront 3 per iteration (trace, resume, spawn)
-    # + 1 advance per iteration + 1 film reduction (+ first spawn)
-    launches = args.steps * (1 if opts.kernel_mode == abi.KERNEL_MEGAKERNEL else (4 * max(1, st_now["iterations"]) + 3))
-    e2e = paths * args.steps * world / (e2e_ms / 1e3) / 1e6
+    value = job_throughput(paths, args.steps, world, total_ms)
+    launches = int(sum(s_["launches"] for s_ in per_step))
+    e2e = job_throughput(paths, args.steps, world, e2e_ms)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
     pk = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)
-    node_b, tri_b = stats["node_bytes"], stats["tri_record_bytes"]
-    alg_bytes = stats["nodes_visited"] * node_b + stats["tris_tested"] * tri_b + paths * 16
     mean_kernel_s = float(np.mean(kernel_ms)) / 1e3
-    achieved = alg_bytes / mean_kernel_s / 1e9
-    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": NCU_TRAFFIC_PER_LAUNCH,
-            "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
-            "algorithmic_bytes_per_launch": alg_bytes, "nodes_visited": stats["nodes_visited"],
-            "tris_tested": stats["tris_tested"], "rays": stats["rays"],
-            "mrays_per_s": stats["rays"] / mean_kernel_s / 1e6, "kernel_ms": float(np.mean(kernel_ms))}
+    kernels = kernel_table(per_step, stats, paths, kernel_ms, opts.kernel_mode == abi.KERNEL_MEGAKERNEL)
+    dom = max(kernels, key=lambda n_: kernels[n_]["ms"])
+    kd = kernels[dom]
+    per_unit = NCU_DRAM_BYTES_PER_UNIT.get(dom)
+    traffic = per_unit * kd["units"] / max(1.0, kd["launches"]) if per_unit else None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": kd["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+            "frac": kd["achieved_gbs"] / hbm, "traffic": traffic,
+            "peak_source": "measured (hbm_gbs)" if "hbm_gbs" in pk else "fallback",
+            "algorithmic_bytes_per_launch": kd["alg_bytes"] / max(1.0, kd["launches"]),
+            "avg_launch_ms": kd["ms"] / max(1.0, kd["launches"]),
+            "kernels": kernels, "nodes_visited": stats["nodes_visited"], "tris_tested": stats["tris_tested"],
+            "rays": stats["rays"], "mrays_per_s": stats["rays"] / mean_kernel_s / 1e6,
+            "step_ms": float(np.mean(kernel_ms))}
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(sb, cam, opts, args.cpu_seconds)
@@ -277,8 +327,6 @@ def main():
             "config": cfg, "parallelism": "replicas" if world > 1 else "single GPU",
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": W * H * 16, "d2h_bytes_per_step": W * H * 16},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
-    if breakdown:
-        line["wavefront_breakdown"] = breakdown
     print(json.dumps(line))
     r.close()
     if dist:

@@ -271,11 +271,17 @@ typedef struct lgpu_stats {
     uint32_t node_bytes;      /* size of one BVH node record */
     uint32_t tri_record_bytes;/* size of one triangle record */
     uint64_t device_bytes;    /* device memory held by the committed scene */
-    /* wavefront breakdown of the last render, filled when the environment variable
-     * LGPU_PROFILE is set (events around every launch): */
+    /* wavefront breakdown of the last render (lgpu_render, lgpu_render_device, lgpu_render_paths),
+     * timed with CUDA events recorded on the render's stream around every launch: */
     double trace_ms, shade_ms, spawn_ms;
     uint32_t iterations;      /* trace + resume rounds of the last wavefront render */
     uint32_t pool_slots;
+    double stage_ms[6];       /* resume time per stage: primary hit, surface extension, null-surface
+                               * extension, medium extension, visibility, transmittance step */
+    uint64_t resumed[6];      /* paths resumed per stage */
+    uint64_t traced;          /* ray queries answered by the trace kernel */
+    uint64_t spawned;         /* paths started */
+    uint64_t launches;        /* kernels launched by the last render */
 } lgpu_stats;
 
 typedef struct lgpu_context lgpu_context;

@@ -90,7 +90,9 @@ class Stats(C.Structure):
                 ("bvh_bytes", C.c_uint64), ("tri_bytes", C.c_uint64), ("node_bytes", C.c_uint32),
                 ("tri_record_bytes", C.c_uint32), ("device_bytes", C.c_uint64),
                 ("trace_ms", C.c_double), ("shade_ms", C.c_double), ("spawn_ms", C.c_double),
-                ("iterations", C.c_uint32), ("pool_slots", C.c_uint32)]
+                ("iterations", C.c_uint32), ("pool_slots", C.c_uint32), ("stage_ms", C.c_double * 6),
+                ("resumed", C.c_uint64 * 6), ("traced", C.c_uint64), ("spawned", C.c_uint64),
+                ("launches", C.c_uint64)]
 
 
 def render_opts(width, height, spp, max_bounces, min_bounces=3, seed=1, spectral=SPECTRAL_RGB3,

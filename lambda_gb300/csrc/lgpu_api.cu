@@ -57,6 +57,7 @@ struct lgpu_context {
     int *w_resobj = nullptr, *w_qa = nullptr, *w_qb = nullptr, *w_counts = nullptr, *w_free = nullptr;
     unsigned long long *w_next = nullptr;
     int *h_count = nullptr;   /* pinned */
+    cudaEvent_t w_ev[LG_NSEG + 3] = {};
     float4 *w_paths = nullptr;
     size_t w_paths_cap = 0;
     int last_iterations = 0;
@@ -267,7 +268,7 @@ bool validate_scene(const HostScene &H, std::string &why) {
 
 extern "C" {
 
-LGPU_API const char *lgpu_version(void) { return "lambda-gb300 0.1 (sm_103a, BVH2 megakernel)"; }
+LGPU_API const char *lgpu_version(void) { return "lambda-gb300 0.2 (sm_103a, BVH2, wavefront + megakernel)"; }
 
 LGPU_API int lgpu_create(lgpu_context **out, int device) {
     if (!out) return LGPU_ERR_INVALID_ARG;
@@ -299,6 +300,7 @@ LGPU_API void lgpu_destroy(lgpu_context *c) {
     cudaFree(c->d_ids);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (auto &x : c->w_ev) if (x) cudaEventDestroy(x);
     cudaFree(c->w_states); cudaFree(c->w_cold); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
     cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_counts); cudaFree(c->w_next); cudaFree(c->w_paths); cudaFree(c->w_free);
     if (c->h_count) cudaFreeHost(c->h_count);
@@ -859,6 +861,8 @@ int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes, size_t cold_b
     if (e == cudaSuccess && !c->w_counts) e = cudaMalloc(&c->w_counts, (2 * LG_NSEG + 2) * sizeof(int));
     if (e == cudaSuccess && !c->w_next) e = cudaMalloc(&c->w_next, sizeof(unsigned long long));
     if (e == cudaSuccess && !c->h_count) e = cudaMallocHost(&c->h_count, (2 * LG_NSEG + 2) * sizeof(int));
+    for (int k = 0; k < LG_NSEG + 3 && e == cudaSuccess; ++k)
+        if (!c->w_ev[k]) e = cudaEventCreate(&c->w_ev[k]);
     if (e != cudaSuccess) return cuda_fail(c, e, "wavefront pool allocation");
     c->w_slots = slots;
     c->w_state_bytes = state_bytes;
@@ -911,64 +915,79 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     cudaError_t e = resume((int)slots, 2);
     if (e != cudaSuccess) return cuda_fail(c, e, "wavefront start");
     int iters = 0;
-    static const bool prof = std::getenv("LGPU_PROFILE") != nullptr;
-    static const bool prof_seg = prof && std::string(std::getenv("LGPU_PROFILE")) == "2";
-    static double seg_ms[LG_NSEG] = {0, 0, 0, 0, 0, 0};
-    cudaEvent_t pe[4] = {nullptr, nullptr, nullptr, nullptr};
-    double acc[3] = {0, 0, 0};
-    if (prof) for (auto &x : pe) cudaEventCreate(&x);
+    uint64_t launches = 2;
+    /* events around every launch of an iteration: [0] before trace, [1] after trace, [2 + k] after
+     * the resume of stage k, [2 + LG_NSEG] after the spawn.  They are read after the next count
+     * read-back has synchronised the stream, so timing costs no extra synchronisation. */
+    cudaEvent_t *ev = c->w_ev;
+    int last_seg[LG_NSEG];
+    bool pending = false;
+    auto account = [&]() {
+        if (!pending) return;
+        float t = 0;
+        cudaEventElapsedTime(&t, ev[0], ev[1]);
+        c->stats.trace_ms += t;
+        int prev = 1;
+        for (int k = 0; k < LG_NSEG; ++k) {
+            if (!last_seg[k]) continue;
+            cudaEventElapsedTime(&t, ev[prev], ev[2 + k]);
+            c->stats.stage_ms[k] += t;
+            c->stats.shade_ms += t;
+            prev = 2 + k;
+        }
+        cudaEventElapsedTime(&t, ev[prev], ev[2 + LG_NSEG]);
+        c->stats.spawn_ms += t;
+        pending = false;
+    };
     for (;;) {
         cudaMemcpyAsync(c->h_count, ca, LG_NSEG * sizeof(int), cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(c, e, "wavefront");
+        account();
         int m = 0;
         W.seg_off[0] = 0;
         for (int k = 0; k < LG_NSEG; ++k) { m += c->h_count[k]; W.seg_off[k + 1] = m; }
-        if (m <= 0) break;
+        if (m <= 0) {
+            /* no path in flight: done, unless paths that all ended inside a spawn left some unstarted */
+            unsigned long long next = 0;
+            e = cudaMemcpy(&next, c->w_next, sizeof(next), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return cuda_fail(c, e, "wavefront");
+            if (next >= n) break;
+            W.queue_in = nullptr; W.queue_out = qa; W.count_out = ca;
+            e = resume((int)slots, 2);   /* every slot is idle: spawn into the whole pool again */
+            if (e != cudaSuccess) return cuda_fail(c, e, "wavefront restart");
+            launches += 2;
+            continue;
+        }
         if (++iters > 100000) return fail(c, LGPU_ERR_TIMEOUT, "wavefront did not drain");
         cudaMemsetAsync(cb, 0, LG_NSEG * sizeof(int), st);
         W.queue_in = qa; W.queue_out = qb; W.count_out = cb;
-        if (prof) cudaEventRecord(pe[0], st);
+        cudaEventRecord(ev[0], st);
         e = count ? wave_trace_3_1(W, m, st) : wave_trace_3_0(W, m, st);
-        if (prof) cudaEventRecord(pe[1], st);
-        if (e == cudaSuccess) {
-            /* one resume launch per queue segment: each launch enters the state machine at one
-             * program point, so its warps run the same code (timed separately with LGPU_PROFILE=2) */
-            WaveArgs W0 = W;
-            for (int k = 0; k < LG_NSEG && e == cudaSuccess; ++k) {
-                const int nk = W.seg_off[k + 1] - W.seg_off[k];
-                if (nk <= 0) continue;
-                for (int j = 0; j <= LG_NSEG; ++j) W.seg_off[j] = j <= k ? 0 : 0x7fffffff;
-                W.queue_in = qa + (size_t)k * W.cap;
-                W.cap_in = 0;
-                if (prof_seg) {
-                    cudaEvent_t a, b;
-                    cudaEventCreate(&a); cudaEventCreate(&b);
-                    cudaEventRecord(a, st);
-                    e = resume(nk, 0);
-                    cudaEventRecord(b, st);
-                    cudaEventSynchronize(b);
-                    float t = 0;
-                    cudaEventElapsedTime(&t, a, b);
-                    seg_ms[k] += t;
-                    cudaEventDestroy(a); cudaEventDestroy(b);
-                } else {
-                    e = resume(nk, 0);
-                }
-                W = W0;
-            }
+        cudaEventRecord(ev[1], st);
+        c->stats.traced += (uint64_t)m;
+        launches += 1;
+        /* one resume launch per queue segment: each launch enters the state machine at one
+         * program point, so its warps run the same code */
+        const WaveArgs W0 = W;
+        for (int k = 0; k < LG_NSEG; ++k) {
+            const int nk = W0.seg_off[k + 1] - W0.seg_off[k];
+            last_seg[k] = 0;
+            if (nk <= 0 || e != cudaSuccess) continue;
+            for (int j = 0; j <= LG_NSEG; ++j) W.seg_off[j] = j <= k ? 0 : 0x7fffffff;
+            W.queue_in = qa + (size_t)k * W0.cap;
+            W.cap_in = 0;
+            e = resume(nk, 0);
+            cudaEventRecord(ev[2 + k], st);
+            last_seg[k] = 1;
+            c->stats.resumed[k] += (uint64_t)nk;
+            launches += 1;
+            W = W0;
         }
-        if (prof) cudaEventRecord(pe[2], st);
         if (e == cudaSuccess) e = resume(m, 1);   /* spawn into the slots freed by this resume */
-        if (prof) {
-            cudaEventRecord(pe[3], st);
-            cudaEventSynchronize(pe[3]);
-            float t0 = 0, t1 = 0, t2 = 0;
-            cudaEventElapsedTime(&t0, pe[0], pe[1]);
-            cudaEventElapsedTime(&t1, pe[1], pe[2]);
-            cudaEventElapsedTime(&t2, pe[2], pe[3]);
-            acc[0] += t0; acc[1] += t1; acc[2] += t2;
-        }
+        cudaEventRecord(ev[2 + LG_NSEG], st);
+        launches += 2;
+        pending = true;
         if (e != cudaSuccess) return cuda_fail(c, e, "wavefront iteration");
         std::swap(qa, qb);
         std::swap(ca, cb);
@@ -976,13 +995,8 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     c->last_iterations = iters;
     c->stats.iterations += (uint32_t)iters;
     c->stats.pool_slots = (uint32_t)slots;
-    c->stats.trace_ms += acc[0]; c->stats.shade_ms += acc[1]; c->stats.spawn_ms += acc[2];
-    if (prof) for (auto &x : pe) cudaEventDestroy(x);
-    if (prof_seg) {
-        std::fprintf(stderr, "[lgpu] resume ms per segment (top_hit surf_ext null_ext med_ext vis_occl tr_step):");
-        for (int k = 0; k < LG_NSEG; ++k) { std::fprintf(stderr, " %.1f", seg_ms[k]); seg_ms[k] = 0; }
-        std::fprintf(stderr, "\n");
-    }
+    c->stats.spawned += n;
+    c->stats.launches += launches;
     return LGPU_OK;
 }
 
@@ -1020,6 +1034,7 @@ int wavefront_frame(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_ren
         if (rc) return rc;
         if (film) {
             cudaError_t e = film_reduce(out, film, p0, npx, o->spp, st);
+            c->stats.launches += 1;
             if (e != cudaSuccess) return cuda_fail(c, e, "film reduce");
         }
     }
@@ -1030,6 +1045,8 @@ int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_
                 const uint64_t *ids, uint64_t n, bool count, cudaStream_t s) {
     c->stats.trace_ms = c->stats.shade_ms = c->stats.spawn_ms = 0;
     c->stats.iterations = 0;
+    for (int k = 0; k < 6; ++k) { c->stats.stage_ms[k] = 0; c->stats.resumed[k] = 0; }
+    c->stats.traced = c->stats.spawned = c->stats.launches = 0;
     if (use_wavefront(o)) {
         if (count) cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned long long), s);
         cudaEventRecord(c->ev0, s);
@@ -1061,6 +1078,7 @@ int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_
     cudaEventRecord(c->ev0, s);
     cudaError_t e = launch_render(a);
     if (e != cudaSuccess) return cuda_fail(c, e, "render launch");
+    c->stats.launches += 1;
     cudaEventRecord(c->ev1, s);
     c->stats.paths = n;
     return LGPU_OK;

@@ -39,7 +39,7 @@ __device__ __forceinline__ void hero_to_rgb(const Spec<NS> &L, const Lambda4 &la
 }
 
 template <int NS, bool COUNT>
-__global__ void __launch_bounds__(128) k_render(DeviceScene S, CamParams cam, RenderParams rp, float4 *film,
+__global__ void __launch_bounds__(128) k_render(const __grid_constant__ DeviceScene S, const __grid_constant__ CamParams cam, const __grid_constant__ RenderParams rp, float4 *film,
                                                 float4 *paths_out, const uint64_t *ids, uint64_t n,
                                                 unsigned long long *counters) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(128) k_render(DeviceScene S, CamParams cam, Re
 
 #if LGPU_NS == 3 && LGPU_COUNT == 0
 /* Closest-hit queries for a ray batch (Scene::Intersect restated; tnear = 0, tfar = inf). */
-__global__ void k_intersect(DeviceScene S, const float4 *rays, uint4 *hits, float2 *uvs, uint64_t n) {
+__global__ void k_intersect(const __grid_constant__ DeviceScene S, const float4 *rays, uint4 *hits, float2 *uvs, uint64_t n) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 a = rays[2 * i], b = rays[2 * i + 1];
@@ -179,7 +179,7 @@ __device__ __forceinline__ void warp_stage(PHot<NS> *G, PHot<NS> *sh, int slot, 
 
 /* Continue every slot of the (segmented) input queue until its next query or its end. */
 template <int NS, bool COUNT>
-__global__ void __launch_bounds__(128) k_wave_resume(WaveArgs W, int n) {
+__global__ void __launch_bounds__(128) k_wave_resume(const __grid_constant__ WaveArgs W, int n) {
     extern __shared__ float4 smem4[];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int slot = -1;
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(128) k_wave_resume(WaveArgs W, int n) {
  * warps of a spawn trace neighbouring samples of one pixel.  Slots come from the free list, or from
  * the untouched tail of the pool on the first spawn. */
 template <int NS, bool COUNT>
-__global__ void __launch_bounds__(128) k_wave_spawn(WaveArgs W, int n_max, int fresh) {
+__global__ void __launch_bounds__(128) k_wave_spawn(const __grid_constant__ WaveArgs W, int n_max, int fresh) {
     extern __shared__ float4 smem4[];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nfree = fresh ? n_max : *W.free_count;
@@ -271,7 +271,7 @@ size_t LG_CAT(wave_cold_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PCold<LGP
 #if LGPU_NS == 3
 /* Answer every queued query: closest hit (Scene::Intersect) or occlusion (rtcOccluded1). */
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_wave_trace(WaveArgs W, int n) {
+__global__ void __launch_bounds__(128) k_wave_trace(const __grid_constant__ WaveArgs W, int n) {
     LocalStack stk;   /* measured faster than a shared-memory column stack (L1 serves it) */
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     TravStats st = {0u, 0u, 0u};
