@@ -338,6 +338,28 @@ LGPU_API int lgpu_render_count(lgpu_context *ctx, const lgpu_camera_desc *camera
 LGPU_API int lgpu_intersect(lgpu_context *ctx, const float *rays_dev, uint32_t *hits_dev,
                             float *uv_out_dev, uint64_t n, void *stream);
 
+/* One view of a batched render: a camera with its own film size, samples per pixel, depth and seed.
+ * film_dev is the view's DEVICE film (width * height float4: r, g, b, sample count), which the render
+ * adds into as Film::AddSample does (src/camera/Film.h:30-33). */
+typedef struct lgpu_view_desc {
+    lgpu_camera_desc camera;
+    int32_t width, height, spp, max_bounces;
+    uint32_t seed, sample_offset;
+    float *film_dev;
+} lgpu_view_desc;
+
+/* Render many views of the committed scene in one wavefront (no counterpart in the reference, which
+ * renders one RenderDirective at a time).  Consecutive views are packed into chunks of at most
+ * 2^28 paths that share one pool of path slots, so views too small to fill the GPU are rendered
+ * together; every path gives the same result as in a single-view render (same random numbers), so
+ * each view's film equals the one lgpu_render_device would produce.  opts supplies the shared
+ * settings (integrator, min_bounces, spectral_mode, kernel_mode, pool_slots, block_size); its width,
+ * height, spp, max_bounces, seed and sample_offset are ignored in favour of each view's.
+ * kernel_mode MEGAKERNEL renders the views one launch at a time instead.  Work is issued on
+ * `stream`; the call returns when every film is complete. */
+LGPU_API int lgpu_render_batch(lgpu_context *ctx, const lgpu_view_desc *views, int32_t n_views,
+                               const lgpu_render_opts *opts, void *stream);
+
 /* Fixed-scratch variant of lgpu_render_paths, for callers that must not allocate.
  * No counterpart in the reference, which renders on the CPU.
  *

@@ -17,7 +17,7 @@ LIB_PATH = HERE / "_build" / "liblambda_gpu.so"
 
 EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_scene_commit", "lgpu_render",
            "lgpu_render_device", "lgpu_render_paths", "lgpu_render_count", "lgpu_intersect",
-           "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc"]
+           "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc", "lgpu_render_batch"]
 
 _lib = None
 
@@ -55,6 +55,7 @@ def lib():
         L.lgpu_get_stats.argtypes = [vp, C.POINTER(abi.Stats)]
         L.lgpu_version.restype = C.c_char_p
         L.lgpu_scene_check.argtypes = [C.POINTER(abi.SceneDesc), C.c_char_p, C.c_size_t]
+        L.lgpu_render_batch.argtypes = [vp, C.POINTER(abi.ViewDesc), C.c_int32, C.POINTER(abi.RenderOpts), vp]
         _lib = L
     return _lib
 
@@ -122,6 +123,17 @@ class Renderer:
         cam = camera.desc()
         self._check(lib().lgpu_render_paths(self._h, C.byref(cam), C.byref(opts), _ptr(ids), len(ids), _ptr(outp)))
         return outp
+
+    def render_batch(self, views, opts, stream=None):
+        """Batched render (lgpu_render_batch).  views: list of (camera, width, height, spp,
+        max_bounces, seed, film_ptr) with film_ptr a device address of width*height float4."""
+        arr = (abi.ViewDesc * len(views))()
+        for i, (cam, w, h, spp, depth, seed, film_ptr) in enumerate(views):
+            arr[i].camera = cam.desc()
+            arr[i].width, arr[i].height, arr[i].spp, arr[i].max_bounces = w, h, spp, depth
+            arr[i].seed, arr[i].sample_offset, arr[i].film_dev = seed, 0, film_ptr
+        self._check(lib().lgpu_render_batch(self._h, arr, len(views), C.byref(opts),
+                                            C.c_void_p(stream) if stream else None))
 
     def render_count(self, camera, opts):
         cam = camera.desc()

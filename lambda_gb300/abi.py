@@ -74,6 +74,12 @@ class CameraDesc(C.Structure):
                 ("z_hat", C.c_float * 3), ("fov", C.c_float), ("type", C.c_int32)]
 
 
+class ViewDesc(C.Structure):
+    _fields_ = [("camera", CameraDesc), ("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
+                ("max_bounces", C.c_int32), ("seed", C.c_uint32), ("sample_offset", C.c_uint32),
+                ("film_dev", C.c_void_p)]
+
+
 class RenderOpts(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
                 ("max_bounces", C.c_int32), ("min_bounces", C.c_int32), ("integrator", C.c_int32),

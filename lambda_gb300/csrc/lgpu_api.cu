@@ -58,6 +58,8 @@ struct lgpu_context {
     unsigned long long *w_next = nullptr;
     int *h_count = nullptr;   /* pinned */
     cudaEvent_t w_ev[LG_NSEG + 3] = {};
+    DView *d_views = nullptr;   /* view table of a batched render */
+    size_t views_cap = 0;
     float4 *w_paths = nullptr;
     size_t w_paths_cap = 0;
     int last_iterations = 0;
@@ -301,6 +303,7 @@ LGPU_API void lgpu_destroy(lgpu_context *c) {
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (auto &x : c->w_ev) if (x) cudaEventDestroy(x);
+    cudaFree(c->d_views);
     cudaFree(c->w_states); cudaFree(c->w_cold); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
     cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_counts); cudaFree(c->w_next); cudaFree(c->w_paths); cudaFree(c->w_free);
     if (c->h_count) cudaFreeHost(c->h_count);
@@ -873,7 +876,8 @@ int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes, size_t cold_b
  * radiance per path into paths_out.  Per iteration: one count read-back, then trace, resume,
  * spawn (new paths into freed slots) and advance. */
 int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o, const uint64_t *ids,
-                  uint64_t base, uint64_t n, float4 *paths_out, bool count, cudaStream_t st) {
+                  uint64_t base, uint64_t n, float4 *paths_out, bool count, cudaStream_t st,
+                  const DView *views_dev = nullptr, int n_views = 0) {
     const bool hero = o->spectral_mode == LGPU_SPECTRAL_HERO4;
     const size_t sb = hero ? wave_state_bytes_4_0() : wave_state_bytes_3_0();
     const size_t cbytes = hero ? wave_cold_bytes_4_0() : wave_cold_bytes_3_0();
@@ -896,6 +900,8 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     W.base = base;
     W.ids = ids;
     W.path_out = paths_out;
+    W.views = views_dev;
+    W.n_views = n_views;
     W.counters = c->d_counters;
     W.cap = (int)slots;
     W.cap_in = (int)slots;
@@ -1193,6 +1199,144 @@ LGPU_API int lgpu_intersect(lgpu_context *c, const float *rays_dev, uint32_t *hi
     e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "intersect");
     return LGPU_OK;
+}
+
+}  // extern "C"
+
+/* ------------------------------------------------------------------ batched views
+ *
+ * lgpu_render_batch renders many views of the committed scene -- each with its own camera, film
+ * size, spp, depth and seed -- through one wavefront: consecutive views are packed into chunks of
+ * at most 256 Mi paths, a chunk's paths share one pool of path slots, so small views no longer
+ * leave the GPU idle and the bounce loop runs once per chunk instead of once per view. */
+namespace {
+
+int check_view(lgpu_context *c, const lgpu_view_desc &v) {
+    if (v.width <= 0 || v.height <= 0 || v.spp <= 0) return fail(c, LGPU_ERR_INVALID_ARG, "view width, height and spp must be positive");
+    if (v.max_bounces < 0) return fail(c, LGPU_ERR_INVALID_ARG, "negative bounce count in a view");
+    if ((uint64_t)v.width * v.height > (1ull << 32) - 1) return fail(c, LGPU_ERR_INVALID_ARG, "view film too large");
+    if (!v.film_dev) return fail(c, LGPU_ERR_INVALID_ARG, "null view film");
+    return LGPU_OK;
+}
+
+lgpu_render_opts view_opts(const lgpu_render_opts *o, const lgpu_view_desc &v) {
+    lgpu_render_opts r = *o;
+    r.width = v.width; r.height = v.height; r.spp = v.spp; r.max_bounces = v.max_bounces;
+    r.seed = v.seed; r.sample_offset = v.sample_offset;
+    return r;
+}
+
+/* One chunk of whole views [v0, v1) through one wavefront, then one film reduction per view. */
+int batch_chunk(lgpu_context *c, const lgpu_view_desc *views, int v0, int v1, const lgpu_render_opts *o, cudaStream_t st) {
+    std::vector<DView> table((size_t)(v1 - v0));
+    uint64_t total = 0;
+    for (int v = v0; v < v1; ++v) {
+        const lgpu_render_opts vo = view_opts(o, views[v]);
+        DView &d = table[(size_t)(v - v0)];
+        d.cam = make_cam(&views[v].camera, &vo);
+        d.rp.spp = vo.spp; d.rp.max_bounces = vo.max_bounces; d.rp.min_bounces = vo.min_bounces;
+        d.rp.seed = vo.seed; d.rp.sample_offset = vo.sample_offset;
+        d.first = total;
+        total += (uint64_t)vo.width * vo.height * vo.spp;
+    }
+    if (c->views_cap < table.size()) {
+        cudaFree(c->d_views);
+        c->d_views = nullptr;
+        c->views_cap = 0;
+        cudaError_t e = cudaMalloc(&c->d_views, table.size() * sizeof(DView));
+        if (e != cudaSuccess) return cuda_fail(c, e, "view table");
+        c->views_cap = table.size();
+    }
+    cudaError_t e = cudaMemcpyAsync(c->d_views, table.data(), table.size() * sizeof(DView), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "view table upload");
+    int rc = ensure_paths(c, total);
+    if (rc) return rc;
+    const lgpu_render_opts vo0 = view_opts(o, views[v0]);
+    rc = run_wavefront(c, &views[v0].camera, &vo0, nullptr, 0, total, c->w_paths, false, st, c->d_views, v1 - v0);
+    if (rc) return rc;
+    for (int v = v0; v < v1; ++v) {
+        const uint64_t px = (uint64_t)views[v].width * views[v].height;
+        e = film_reduce(c->w_paths + table[(size_t)(v - v0)].first, reinterpret_cast<float4 *>(views[v].film_dev), 0, px,
+                        views[v].spp, st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "film reduce");
+        c->stats.launches += 1;
+    }
+    return LGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+LGPU_API int lgpu_render_batch(lgpu_context *c, const lgpu_view_desc *views, int32_t n_views, const lgpu_render_opts *o,
+                               void *stream) {
+    if (!c || !o || n_views < 0 || (n_views > 0 && !views)) return LGPU_ERR_INVALID_ARG;
+    if (!c->have_scene) return fail(c, LGPU_ERR_NO_SCENE, "no committed scene");
+    if (o->integrator != LGPU_INTEGRATOR_GPU_MISVOLPATH && o->integrator != LGPU_INTEGRATOR_VOLPATH)
+        return fail(c, LGPU_ERR_INVALID_ARG, "integrator not available on the GPU path");
+    if (o->min_bounces < 0) return fail(c, LGPU_ERR_INVALID_ARG, "negative bounce count");
+    for (int v = 0; v < n_views; ++v) {
+        int r = check_view(c, views[v]);
+        if (r) return r;
+    }
+    cudaSetDevice(c->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    c->stats.trace_ms = c->stats.shade_ms = c->stats.spawn_ms = 0;
+    c->stats.iterations = 0;
+    for (int k = 0; k < 6; ++k) { c->stats.stage_ms[k] = 0; c->stats.resumed[k] = 0; }
+    c->stats.traced = c->stats.spawned = c->stats.launches = 0;
+    cudaEventRecord(c->ev0, st);
+    uint64_t all = 0;
+    if (o->kernel_mode == LGPU_KERNEL_MEGAKERNEL) {
+        /* one megakernel launch per view (the unbatched scheme) */
+        for (int v = 0; v < n_views; ++v) {
+            const lgpu_render_opts vo = view_opts(o, views[v]);
+            const uint64_t n = (uint64_t)vo.width * vo.height * vo.spp;
+            LaunchArgs a;
+            a.S = c->S;
+            a.cam = make_cam(&views[v].camera, &vo);
+            a.rp.spp = vo.spp; a.rp.max_bounces = vo.max_bounces; a.rp.min_bounces = vo.min_bounces;
+            a.rp.seed = vo.seed; a.rp.sample_offset = vo.sample_offset;
+            a.film = reinterpret_cast<float4 *>(views[v].film_dev);
+            a.paths_out = nullptr; a.ids = nullptr; a.n = n; a.counters = c->d_counters;
+            a.hero = vo.spectral_mode == LGPU_SPECTRAL_HERO4;
+            a.count = false;
+            a.stream = st;
+            cudaError_t e = launch_render(a);
+            if (e != cudaSuccess) return cuda_fail(c, e, "render launch");
+            c->stats.launches += 1;
+            all += n;
+        }
+    } else {
+        const uint64_t max_chunk = (uint64_t)1 << 28;
+        int v0 = 0;
+        uint64_t acc = 0;
+        for (int v = 0; v <= n_views; ++v) {
+            const uint64_t n = v < n_views ? (uint64_t)views[v].width * views[v].height * views[v].spp : 0;
+            if (v == n_views || (acc > 0 && acc + n > max_chunk) || n > max_chunk) {
+                if (v > v0 && acc > 0) {
+                    int r = batch_chunk(c, views, v0, v, o, st);
+                    if (r) return r;
+                }
+                v0 = v;
+                acc = 0;
+                if (v < n_views && n > max_chunk) {   /* a view larger than a chunk: pixel chunks of its own */
+                    const lgpu_render_opts vo = view_opts(o, views[v]);
+                    int r = wavefront_frame(c, &views[v].camera, &vo, reinterpret_cast<float4 *>(views[v].film_dev), nullptr,
+                                            false, st);
+                    if (r) return r;
+                    v0 = v + 1;
+                    all += n;
+                    continue;
+                }
+            }
+            acc += n;
+            all += n;
+        }
+    }
+    cudaEventRecord(c->ev1, st);
+    c->stats.paths = all;
+    return finish_timing(c);
 }
 
 }  // extern "C"

@@ -16,6 +16,13 @@ struct RenderParams {
     int spp, max_bounces, min_bounces;
     uint32_t seed, sample_offset;
 };
+/* One view of a batched render: its camera and parameters, and the index of its first path within
+ * the chunk of views being rendered (paths of a view are pixel-major, spp per pixel). */
+struct DView {
+    CamParams cam;
+    RenderParams rp;
+    uint64_t first;
+};
 struct LaunchArgs {
     DeviceScene S;
     CamParams cam;

@@ -54,7 +54,7 @@ template <int NS>
 struct __align__(16) PHot {
     uint64_t out;                 /* output index of the path (within the chunk) */
     uint32_t key, dim;
-    uint32_t pixel, pad0;
+    uint32_t pixel, view;         /* view: index into WaveArgs::views (batched renders) */
     float lam[4];
     int pc, bounces, nullCrossings, scatterIntersect;
     Spec<NS> L, beta;
@@ -116,6 +116,8 @@ struct WaveArgs {
     uint64_t base;                /* path id of chunk index 0 (when ids == nullptr) */
     const uint64_t *ids;          /* explicit path ids or nullptr */
     float4 *path_out;             /* radiance per chunk index, w = random numbers drawn */
+    const DView *views;           /* batched views of this chunk (nullptr: one view, cam + rp) */
+    int n_views;
     unsigned long long *counters; /* traversal counters (COUNT variant) */
 };
 
@@ -341,9 +343,23 @@ struct Wave {
 
     /* Start path number `idx` of the chunk in this slot (camera ray, Render.cpp:55-56 + Camera.cpp:41-44). */
     __device__ void start_path(uint64_t idx) {
-        const RenderParams &rp = W.rp;
-        const CamParams &cam = W.cam;
-        const uint64_t pid = W.ids ? W.ids[idx] : W.base + idx;
+        int view = 0;
+        uint64_t pid;
+        if (W.views) {
+            /* last view whose first path is <= idx (views are in path order) */
+            int lo = 0, hi = W.n_views - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (W.views[mid].first <= idx) lo = mid; else hi = mid - 1;
+            }
+            view = lo;
+            pid = idx - W.views[view].first;
+        } else {
+            pid = W.ids ? W.ids[idx] : W.base + idx;
+        }
+        const RenderParams &rp = W.views ? W.views[view].rp : W.rp;
+        const CamParams &cam = W.views ? W.views[view].cam : W.cam;
+        s.view = (uint32_t)view;
         const uint32_t pixel = (uint32_t)(pid / (uint64_t)rp.spp);
         const uint32_t sidx = (uint32_t)(pid % (uint64_t)rp.spp) + rp.sample_offset;
         const uint32_t x = pixel % (uint32_t)cam.W, y = pixel / (uint32_t)cam.W;
@@ -381,7 +397,8 @@ struct Wave {
     /* Run the state machine until the path issues a query or ends. */
     __device__ void run() {
         const DeviceScene &S = W.S;
-        const int maxB = W.rp.max_bounces, minB = W.rp.min_bounces;
+        const RenderParams &rp = W.views ? W.views[s.view].rp : W.rp;
+        const int maxB = rp.max_bounces, minB = rp.min_bounces;
         for (int guard = 0; guard < 4096; ++guard) {
             switch (s.pc) {
             case PC_LOOP: {
