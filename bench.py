@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--spp", type=int, default=64)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--mode", default="auto", choices=["auto", "megakernel", "wavefront"])
+    p.add_argument("--mode", default="auto", choices=["auto", "megakernel", "wavefront", "graph"])
     p.add_argument("--pool", type=int, default=0, help="wavefront path-slot pool size (0 = default)")
     return p.parse_args()
 
@@ -182,6 +182,10 @@ def kernel_table(per_step, stats, paths, kernel_ms, megakernel):
     if megakernel:
         k["k_render"] = {"ms": float(np.mean(kernel_ms)), "launches": 1.0, "units": float(paths),
                          "alg_bytes": float(trav_bytes + paths * 16)}
+    elif mean(lambda s_: s_["trace_ms"]) == 0.0:
+        # graph-replayed bounce loop: no per-launch events; the whole frame against its traversal bytes
+        k["wavefront_graph"] = {"ms": float(np.mean(kernel_ms)), "launches": mean(lambda s_: s_["launches"]),
+                                "units": float(stats["rays"]), "alg_bytes": float(trav_bytes)}
     else:
         iters = mean(lambda s_: s_["iterations"])
         resumed = mean(lambda s_: sum(s_["resumed"]))
@@ -241,7 +245,8 @@ def main():
     torch.cuda.set_device(dev)
     sb, cam, opts = configs.terrain(args.width, args.height, args.spp, 6)
     opts.seed = replica_seed(rank)
-    opts.kernel_mode = {"auto": abi.KERNEL_AUTO, "megakernel": abi.KERNEL_MEGAKERNEL, "wavefront": abi.KERNEL_WAVEFRONT}[args.mode]
+    opts.kernel_mode = {"auto": abi.KERNEL_AUTO, "megakernel": abi.KERNEL_MEGAKERNEL, "wavefront": abi.KERNEL_WAVEFRONT,
+                        "graph": abi.KERNEL_WAVEFRONT_GRAPH}[args.mode]
     opts.pool_slots = args.pool
     r = lg.Renderer(sb, device=dev)
     W, H, spp = opts.width, opts.height, opts.spp

@@ -246,7 +246,7 @@ typedef struct lgpu_render_opts {
     int32_t spectral_mode;    /* lgpu_spectral_mode */
     uint32_t seed;            /* counter-based RNG key */
     uint32_t sample_offset;   /* first sample index: resume = same seed, offset = samples done */
-    int32_t block_size;       /* 0 = autotuned default */
+    int32_t block_size;       /* threads per block of the wavefront trace kernel: 64, 128, 256 or 512 (0 = 128) */
     int32_t kernel_mode;      /* lgpu_kernel_mode */
     int32_t pool_slots;       /* wavefront path-slot pool size, 0 = default (4 Mi slots) */
 } lgpu_render_opts;
@@ -255,7 +255,10 @@ typedef struct lgpu_render_opts {
 typedef enum lgpu_kernel_mode {
     LGPU_KERNEL_AUTO = 0,        /* wavefront */
     LGPU_KERNEL_MEGAKERNEL = 1,  /* one thread runs a whole path */
-    LGPU_KERNEL_WAVEFRONT = 2    /* path state machine + separate traversal kernels */
+    LGPU_KERNEL_WAVEFRONT = 2,   /* path state machine + separate traversal kernels */
+    LGPU_KERNEL_WAVEFRONT_GRAPH = 3  /* the same kernels over resident grids, reading their queue sizes
+                                      * on the device; the bounce loop is a CUDA graph replayed by
+                                      * the host (no per-launch timing in lgpu_stats) */
 } lgpu_kernel_mode;
 
 /* Per-render statistics.  Traversal counters are filled only by lgpu_render_count. */

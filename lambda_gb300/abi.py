@@ -87,7 +87,7 @@ class RenderOpts(C.Structure):
                 ("block_size", C.c_int32), ("kernel_mode", C.c_int32), ("pool_slots", C.c_int32)]
 
 
-KERNEL_AUTO, KERNEL_MEGAKERNEL, KERNEL_WAVEFRONT = 0, 1, 2
+KERNEL_AUTO, KERNEL_MEGAKERNEL, KERNEL_WAVEFRONT, KERNEL_WAVEFRONT_GRAPH = 0, 1, 2, 3
 
 
 class Stats(C.Structure):

@@ -59,6 +59,7 @@ struct lgpu_context {
     int *h_count = nullptr;   /* pinned */
     cudaEvent_t w_ev[LG_NSEG + 3] = {};
     DView *d_views = nullptr;   /* view table of a batched render */
+    cudaStream_t graph_stream = nullptr;   /* graph-mode work when the caller passes the default stream */
     size_t views_cap = 0;
     float4 *w_paths = nullptr;
     size_t w_paths_cap = 0;
@@ -304,6 +305,7 @@ LGPU_API void lgpu_destroy(lgpu_context *c) {
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (auto &x : c->w_ev) if (x) cudaEventDestroy(x);
     cudaFree(c->d_views);
+    if (c->graph_stream) cudaStreamDestroy(c->graph_stream);
     cudaFree(c->w_states); cudaFree(c->w_cold); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
     cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_counts); cudaFree(c->w_next); cudaFree(c->w_paths); cudaFree(c->w_free);
     if (c->h_count) cudaFreeHost(c->h_count);
@@ -872,6 +874,83 @@ int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes, size_t cold_b
     return LGPU_OK;
 }
 
+/* Bounce loop as a CUDA graph: two iterations (queue A -> B -> A) of device-driven launches -- the
+ * trace, resume and spawn kernels read their queue sizes on the device and run over resident
+ * grids -- are captured once per call and replayed; the host reads the queue sizes back only
+ * after every second replay to detect the end.  Per-launch timing is not recorded in this mode. */
+int run_graph_loop(lgpu_context *c, WaveArgs &W, bool hero, size_t slots, uint64_t n, int tblock, int *qa, int *qb,
+                   int *ca, int *cb, cudaStream_t user_st) {
+    /* the legacy default stream cannot be captured: work on a stream of the context instead, after
+     * everything already queued on the caller's stream (the loop ends synchronised) */
+    cudaStream_t st = user_st;
+    if (!st) {
+        if (!c->graph_stream) {
+            cudaError_t e0 = cudaStreamCreateWithFlags(&c->graph_stream, cudaStreamNonBlocking);
+            if (e0 != cudaSuccess) return cuda_fail(c, e0, "graph stream");
+        }
+        cudaError_t e0 = cudaStreamSynchronize(user_st);
+        if (e0 != cudaSuccess) return cuda_fail(c, e0, "graph stream");
+        st = c->graph_stream;
+    }
+    auto resume = [&](int m, int mode) { return hero ? wave_resume_4_0(W, m, mode, st) : wave_resume_3_0(W, m, mode, st); };
+    cudaError_t e = wave_trace_3_0(W, 0, st, tblock);   /* set-up of the resident grid, before capture */
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph set-up");
+    const WaveArgs W0 = W;
+    auto iteration = [&](int *qin, int *cin, int *qout, int *cout) {
+        cudaError_t r = cudaMemsetAsync(cout, 0, LG_NSEG * sizeof(int), st);
+        W = W0;
+        W.queue_in = qin; W.count_in = cin; W.queue_out = qout; W.count_out = cout; W.cap_in = W.cap;
+        if (r == cudaSuccess) r = wave_trace_3_0(W, -1, st, tblock);
+        for (int k = 0; k < LG_NSEG && r == cudaSuccess; ++k) { W.seg_sel = k; r = resume(-1, 0); }
+        W.seg_sel = 0;
+        if (r == cudaSuccess) r = resume(-(int)slots, 1);
+        return r;
+    };
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t r = iteration(qa, ca, qb, cb);
+        if (r == cudaSuccess) r = iteration(qb, cb, qa, ca);
+        e = cudaStreamEndCapture(st, &g);
+        if (e == cudaSuccess) e = r;
+    }
+    W = W0;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) { if (ge) cudaGraphExecDestroy(ge); return cuda_fail(c, e, "graph capture"); }
+    uint64_t launches = 2, replays = 0;
+    int rc = LGPU_OK;
+    for (;;) {
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) { e = cudaGraphLaunch(ge, st); ++replays; }
+        launches += 2 * 2 * (1 + LG_NSEG + 2);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_count, ca, LG_NSEG * sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { rc = cuda_fail(c, e, "graph replay"); break; }
+        int m = 0;
+        for (int k = 0; k < LG_NSEG; ++k) m += c->h_count[k];
+        if (m > 0) {
+            if (replays > 200000) { rc = fail(c, LGPU_ERR_TIMEOUT, "wavefront did not drain"); break; }
+            continue;
+        }
+        unsigned long long next = 0;
+        e = cudaMemcpy(&next, c->w_next, sizeof(next), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { rc = cuda_fail(c, e, "graph replay"); break; }
+        if (next >= n) break;
+        W.queue_in = nullptr; W.queue_out = qa; W.count_out = ca; W.count_in = nullptr;
+        e = resume((int)slots, 2);   /* every slot is idle: spawn into the whole pool again */
+        W = W0;
+        launches += 2;
+        if (e != cudaSuccess) { rc = cuda_fail(c, e, "graph restart"); break; }
+    }
+    cudaGraphExecDestroy(ge);
+    c->stats.iterations += (uint32_t)(2 * replays);
+    c->stats.pool_slots = (uint32_t)slots;
+    c->stats.spawned += n;
+    c->stats.launches += launches;
+    return rc;
+}
+
 /* Run the wavefront over `n` paths (chunk indices 0..n-1 = path ids base.. or ids[]), writing
  * radiance per path into paths_out.  Per iteration: one count read-back, then trace, resume,
  * spawn (new paths into freed slots) and advance. */
@@ -920,6 +999,9 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     W.queue_in = nullptr; W.queue_out = qa; W.count_out = ca;
     cudaError_t e = resume((int)slots, 2);
     if (e != cudaSuccess) return cuda_fail(c, e, "wavefront start");
+    const int tblock = o->block_size > 0 ? o->block_size : 128;
+    if (o->kernel_mode == LGPU_KERNEL_WAVEFRONT_GRAPH && !count)
+        return run_graph_loop(c, W, hero, slots, n, tblock, qa, qb, ca, cb, st);
     int iters = 0;
     uint64_t launches = 2;
     /* events around every launch of an iteration: [0] before trace, [1] after trace, [2 + k] after
@@ -969,7 +1051,7 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
         cudaMemsetAsync(cb, 0, LG_NSEG * sizeof(int), st);
         W.queue_in = qa; W.queue_out = qb; W.count_out = cb;
         cudaEventRecord(ev[0], st);
-        e = count ? wave_trace_3_1(W, m, st) : wave_trace_3_0(W, m, st);
+        e = count ? wave_trace_3_1(W, m, st, tblock) : wave_trace_3_0(W, m, st, tblock);
         cudaEventRecord(ev[1], st);
         c->stats.traced += (uint64_t)m;
         launches += 1;
@@ -1241,6 +1323,7 @@ int batch_chunk(lgpu_context *c, const lgpu_view_desc *views, int v0, int v1, co
     }
     if (c->views_cap < table.size()) {
         cudaFree(c->d_views);
+    if (c->graph_stream) cudaStreamDestroy(c->graph_stream);
         c->d_views = nullptr;
         c->views_cap = 0;
         cudaError_t e = cudaMalloc(&c->d_views, table.size() * sizeof(DView));

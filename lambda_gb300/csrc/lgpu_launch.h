@@ -49,8 +49,8 @@ cudaError_t wave_resume_3_0(const WaveArgs &W, int n, int start_new, cudaStream_
 cudaError_t wave_resume_3_1(const WaveArgs &W, int n, int start_new, cudaStream_t st);
 cudaError_t wave_resume_4_0(const WaveArgs &W, int n, int start_new, cudaStream_t st);
 cudaError_t wave_resume_4_1(const WaveArgs &W, int n, int start_new, cudaStream_t st);
-cudaError_t wave_trace_3_0(const WaveArgs &W, int n, cudaStream_t st);
-cudaError_t wave_trace_3_1(const WaveArgs &W, int n, cudaStream_t st);
+cudaError_t wave_trace_3_0(const WaveArgs &W, int n, cudaStream_t st, int block = 128);
+cudaError_t wave_trace_3_1(const WaveArgs &W, int n, cudaStream_t st, int block = 128);
 size_t wave_state_bytes_3_0();
 size_t wave_cold_bytes_3_0();
 size_t wave_cold_bytes_4_0();

@@ -9,6 +9,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "lgpu_integrator.cuh"
 #include "lgpu_launch.h"
 #include "lgpu_wavefront.cuh"
@@ -177,65 +179,76 @@ __device__ __forceinline__ void warp_stage(PHot<NS> *G, PHot<NS> *sh, int slot, 
     __syncwarp();
 }
 
-/* Continue every slot of the (segmented) input queue until its next query or its end. */
+/* Continue every slot of the (segmented) input queue until its next query or its end.  Grid-stride:
+ * a launch sized to the queue runs the loop body once per thread; a device-driven launch (fixed
+ * grid, n read from W.count_in) loops.  The loop bound is block-uniform, so warps stay converged
+ * for the warp-cooperative staging. */
 template <int NS, bool COUNT>
 __global__ void __launch_bounds__(128) k_wave_resume(const __grid_constant__ WaveArgs W, int n) {
     extern __shared__ float4 smem4[];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int slot = -1;
-    if (i < n) {
-        int seg = 0;
-#pragma unroll
-        for (int k = 1; k < LG_NSEG; ++k) seg += (i >= W.seg_off[k]) ? 1 : 0;
-        slot = W.queue_in[seg * W.cap_in + (i - W.seg_off[seg])];
-    }
+    if (W.count_in) n = W.count_in[W.seg_sel];
     PHot<NS> *G = reinterpret_cast<PHot<NS> *>(W.states);
     PHot<NS> *sh = reinterpret_cast<PHot<NS> *>(smem4) + (threadIdx.x & ~31);
-    warp_stage<NS>(G, sh, slot, true);
-    int keep = -1;
-    if (slot >= 0) {
-        PHot<NS> &s = sh[threadIdx.x & 31];
-        PCold<NS> &c = reinterpret_cast<PCold<NS> *>(W.cold)[slot];
-        Wave<NS, COUNT> w{W, s, c, slot};
-        w.rng.key = s.key;
-        w.rng.dim = s.dim;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        int slot = -1;
+        if (i < n) {
+            if (W.count_in) {
+                slot = W.queue_in[W.seg_sel * W.cap + i];
+            } else {
+                int seg = 0;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) w.lam.l[k] = s.lam[k];
-        w.run();
-        if (s.pc == PC_DONE) { w.finish(); push_free(W, slot); }
-        else { wave_save(w, s); keep = slot; }
+                for (int k = 1; k < LG_NSEG; ++k) seg += (i >= W.seg_off[k]) ? 1 : 0;
+                slot = W.queue_in[seg * W.cap_in + (i - W.seg_off[seg])];
+            }
+        }
+        warp_stage<NS>(G, sh, slot, true);
+        int keep = -1;
+        if (slot >= 0) {
+            PHot<NS> &s = sh[threadIdx.x & 31];
+            PCold<NS> &c = reinterpret_cast<PCold<NS> *>(W.cold)[slot];
+            Wave<NS, COUNT> w{W, s, c, slot};
+            w.rng.key = s.key;
+            w.rng.dim = s.dim;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) w.lam.l[k] = s.lam[k];
+            w.run();
+            if (s.pc == PC_DONE) { w.finish(); push_free(W, slot); }
+            else { wave_save(w, s); keep = slot; }
+        }
+        __syncwarp();
+        warp_stage<NS>(G, sh, keep, false);
     }
-    __syncwarp();
-    warp_stage<NS>(G, sh, keep, false);
 }
 
 /* Start new paths in free slots: consecutive path ids go to consecutive free-list entries, so the
  * warps of a spawn trace neighbouring samples of one pixel.  Slots come from the free list, or from
- * the untouched tail of the pool on the first spawn. */
+ * the untouched tail of the pool on the first spawn.  Grid-stride like k_wave_resume. */
 template <int NS, bool COUNT>
 __global__ void __launch_bounds__(128) k_wave_spawn(const __grid_constant__ WaveArgs W, int n_max, int fresh) {
     extern __shared__ float4 smem4[];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nfree = fresh ? n_max : *W.free_count;
     const unsigned long long next = *W.next_path;
     const unsigned long long left = next < W.n_paths ? W.n_paths - next : 0ull;
     const int m = (int)(nfree < (int)min(left, (unsigned long long)0x7fffffff) ? nfree : (int)left);
-    if (blockIdx.x * blockDim.x >= m) return;   /* whole block idle */
-    int keep = -1;
     PHot<NS> *G = reinterpret_cast<PHot<NS> *>(W.states);
     PHot<NS> *sh = reinterpret_cast<PHot<NS> *>(smem4) + (threadIdx.x & ~31);
-    if (i < m) {
-        const int slot = fresh ? i : W.free_list[i];
-        PHot<NS> &s = sh[threadIdx.x & 31];
-        PCold<NS> &c = reinterpret_cast<PCold<NS> *>(W.cold)[slot];
-        Wave<NS, COUNT> w{W, s, c, slot};
-        w.start_path(next + (uint64_t)i);
-        w.run();
-        if (s.pc == PC_DONE) w.finish();   /* slot idles until a later spawn reuses it */
-        else { wave_save(w, s); keep = slot; }
+    for (int base = blockIdx.x * blockDim.x; base < m; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        int keep = -1;
+        if (i < m) {
+            const int slot = fresh ? i : W.free_list[i];
+            PHot<NS> &s = sh[threadIdx.x & 31];
+            PCold<NS> &c = reinterpret_cast<PCold<NS> *>(W.cold)[slot];
+            Wave<NS, COUNT> w{W, s, c, slot};
+            w.start_path(next + (uint64_t)i);
+            w.run();
+            if (s.pc == PC_DONE) w.finish();   /* slot idles until a later spawn reuses it */
+            else { wave_save(w, s); keep = slot; }
+        }
+        __syncwarp();
+        warp_stage<NS>(G, sh, keep, false);
     }
-    __syncwarp();
-    warp_stage<NS>(G, sh, keep, false);
 }
 /* next_path += paths started by the last spawn; clear the free list. */
 static __global__ void k_wave_advance(WaveArgs W, int n_max, int fresh) {
@@ -247,6 +260,16 @@ static __global__ void k_wave_advance(WaveArgs W, int n_max, int fresh) {
     *W.free_count = 0;
 }
 
+/* Blocks of a device-driven launch: enough to fill every SM at the kernel's occupancy. */
+template <typename K>
+static int resident_grid(K kernel, int block, size_t smem) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+    return std::max(1, sms * std::max(1, per_sm));
+}
+
 cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, int start_new, cudaStream_t st) {
     const size_t smem = 128 * sizeof(PHot<LGPU_NS>);
     static bool configured = false;
@@ -255,14 +278,23 @@ cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, 
         cudaFuncSetAttribute(k_wave_spawn<LGPU_NS, LGPU_COUNT != 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured = true;
     }
+    static int grid_resume = 0, grid_spawn = 0;
+    if (!grid_resume) {
+        grid_resume = resident_grid(k_wave_resume<LGPU_NS, LGPU_COUNT != 0>, 128, smem);
+        grid_spawn = resident_grid(k_wave_spawn<LGPU_NS, LGPU_COUNT != 0>, 128, smem);
+    }
+    /* n < 0: device-driven launch over a fixed resident grid (sizes read on the device) */
     if (start_new) {
-        /* spawn into up to n slots (fresh pool or free list), then advance the path counter */
-        if (n > 0) k_wave_spawn<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, smem, st>>>(W, n, start_new == 2);
-        k_wave_advance<<<1, 1, 0, st>>>(W, n, start_new == 2);
+        /* spawn into up to |n| slots (fresh pool or free list), then advance the path counter */
+        const int nm = n < 0 ? -n : n;
+        const int blocks = n < 0 ? std::min(grid_spawn, (nm + 127) / 128) : (n + 127) / 128;
+        if (nm > 0) k_wave_spawn<LGPU_NS, LGPU_COUNT != 0><<<blocks, 128, smem, st>>>(W, nm, start_new == 2);
+        k_wave_advance<<<1, 1, 0, st>>>(W, nm, start_new == 2);
         return cudaGetLastError();
     }
-    if (n <= 0) return cudaSuccess;
-    k_wave_resume<LGPU_NS, LGPU_COUNT != 0><<<(n + 127) / 128, 128, smem, st>>>(W, n);
+    if (n == 0) return cudaSuccess;
+    const int blocks = n < 0 ? grid_resume : (n + 127) / 128;
+    k_wave_resume<LGPU_NS, LGPU_COUNT != 0><<<blocks, 128, smem, st>>>(W, n < 0 ? 0 : n);
     return cudaGetLastError();
 }
 size_t LG_CAT(wave_state_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PHot<LGPU_NS>); }
@@ -271,15 +303,27 @@ size_t LG_CAT(wave_cold_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PCold<LGP
 #if LGPU_NS == 3
 /* Answer every queued query: closest hit (Scene::Intersect) or occlusion (rtcOccluded1). */
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_wave_trace(const __grid_constant__ WaveArgs W, int n) {
+__global__ void __launch_bounds__(512) k_wave_trace(const __grid_constant__ WaveArgs W, int n) {
     LocalStack stk;   /* measured faster than a shared-memory column stack (L1 serves it) */
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    TravStats st = {0u, 0u, 0u};
-    if (i < n) {
-        int seg = 0;
+    int off[LG_NSEG + 1];
+    if (W.count_in) {   /* device-driven: segment sizes from the device */
+        off[0] = 0;
 #pragma unroll
-        for (int k = 1; k < LG_NSEG; ++k) seg += (i >= W.seg_off[k]) ? 1 : 0;
-        const int slot = W.queue_in[seg * W.cap_in + (i - W.seg_off[seg])];
+        for (int k = 0; k < LG_NSEG; ++k) off[k + 1] = off[k] + W.count_in[k];
+        n = off[LG_NSEG];
+    } else {
+#pragma unroll
+        for (int k = 0; k <= LG_NSEG; ++k) off[k] = W.seg_off[k];
+    }
+    const int stride = W.count_in ? W.cap : W.cap_in;
+    TravStats st = {0u, 0u, 0u};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int seg = 0, first = 0;
+#pragma unroll
+        for (int k = 1; k < LG_NSEG; ++k) seg += (i >= off[k]) ? 1 : 0;
+#pragma unroll
+        for (int k = 0; k < LG_NSEG; ++k) first = (seg == k) ? off[k] : first;
+        const int slot = W.queue_in[seg * stride + (i - first)];
         const float4 o = W.qo[slot], d = W.qd[slot];
         HitRec hr;
         if (__float_as_int(d.w) == Q_CLOSEST) {
@@ -302,10 +346,16 @@ __global__ void __launch_bounds__(128) k_wave_trace(const __grid_constant__ Wave
         }
     }
 }
-cudaError_t LG_CAT(wave_trace_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    const int bs = 128;
-    k_wave_trace<LGPU_COUNT != 0><<<(n + bs - 1) / bs, bs, 0, st>>>(W, n);
+/* n < 0: device-driven launch over a resident grid (the queue sizes are read on the device);
+ * n == 0: set-up of the resident grid only.  block: 64, 128, 256 or 512 threads. */
+cudaError_t LG_CAT(wave_trace_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, cudaStream_t st, int block) {
+    const int bs = (block == 64 || block == 256 || block == 512) ? block : 128;
+    static int grid[4] = {0, 0, 0, 0};
+    const int gi = bs == 64 ? 0 : bs == 128 ? 1 : bs == 256 ? 2 : 3;
+    if (!grid[gi]) grid[gi] = resident_grid(k_wave_trace<LGPU_COUNT != 0>, bs, 0);
+    if (n == 0) return cudaSuccess;
+    const int blocks = n < 0 ? grid[gi] : (n + bs - 1) / bs;
+    k_wave_trace<LGPU_COUNT != 0><<<blocks, bs, 0, st>>>(W, n < 0 ? 0 : n);
     return cudaGetLastError();
 }
 #endif

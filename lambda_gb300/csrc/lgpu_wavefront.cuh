@@ -118,6 +118,10 @@ struct WaveArgs {
     float4 *path_out;             /* radiance per chunk index, w = random numbers drawn */
     const DView *views;           /* batched views of this chunk (nullptr: one view, cam + rp) */
     int n_views;
+    /* Device-driven launches (bounce loop captured in a CUDA graph): the kernels read the sizes of
+     * the input queue segments from count_in instead of taking them from the host (seg_off, n). */
+    const int *count_in;
+    int seg_sel;                  /* device-driven resume: the one segment this launch continues */
     unsigned long long *counters; /* traversal counters (COUNT variant) */
 };
 

@@ -34,19 +34,21 @@ def _render_alone(torch, r, views, opts):
     return out
 
 
-@pytest.mark.parametrize("pool", [0, 700])
-def test_batch_equals_single_views_cornell(gpu_lib, pool):
+@pytest.mark.parametrize("pool,mode", [(0, 2), (700, 2), (0, 3), (700, 3)],
+                         ids=["host_loop", "host_loop_small_pool", "graph", "graph_small_pool"])
+def test_batch_equals_single_views_cornell(gpu_lib, pool, mode):
     torch = pytest.importorskip("torch")
     from lambda_gb300 import abi, configs
     from lambda_gb300.scene import Camera
     sb, _, opts = configs.cornell(16, 16, 1)
     opts.pool_slots = pool
-    opts.kernel_mode = abi.KERNEL_WAVEFRONT
+    opts.kernel_mode = mode
     views = _views(Camera)
     r = gpu_lib.Renderer(sb)
     try:
         batch = _render_batch(torch, r, views, opts)
         assert r.stats()["paths"] == sum(w * h * spp for (_, w, h, spp, _, _) in views)
+        opts.kernel_mode = abi.KERNEL_WAVEFRONT
         alone = _render_alone(torch, r, views, opts)
         for (cam, w, h, spp, _, _), b, a in zip(views, batch, alone):
             assert np.all(b[..., 3] == spp)

@@ -14,7 +14,7 @@ from tests.parity import path_agreement, sample_ids
 
 pytestmark = pytest.mark.gpu
 
-MODES = pytest.mark.parametrize("mode", [1, 2], ids=["megakernel", "wavefront"])
+MODES = pytest.mark.parametrize("mode", [1, 2, 3], ids=["megakernel", "wavefront", "wavefront_graph"])
 
 
 def _render_both(lg, sb, cam, opts, n):
@@ -94,7 +94,10 @@ def test_wavefront_equals_megakernel_terrain(gpu_lib):
     opts.kernel_mode = 2
     opts.pool_slots = 1000   # small pool: exercises path regeneration
     b = r.render_paths(cam, opts, ids)
+    opts.kernel_mode = 3      # same kernels, device-driven, bounce loop as a CUDA graph
+    c = r.render_paths(cam, opts, ids)
     r.close()
     np.testing.assert_array_equal(a[:, 3], b[:, 3])
     frac, _ = path_agreement(a, b, rel=1e-5)
     assert frac >= 0.999
+    np.testing.assert_array_equal(b, c)
