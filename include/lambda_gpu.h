@@ -253,7 +253,7 @@ typedef struct lgpu_render_opts {
 
 /* Execution scheme of one render.  Both produce the same paths (same random-number order). */
 typedef enum lgpu_kernel_mode {
-    LGPU_KERNEL_AUTO = 0,        /* wavefront */
+    LGPU_KERNEL_AUTO = 0,        /* the lgpu_autotune result if there is one, else wavefront */
     LGPU_KERNEL_MEGAKERNEL = 1,  /* one thread runs a whole path */
     LGPU_KERNEL_WAVEFRONT = 2,   /* path state machine + separate traversal kernels */
     LGPU_KERNEL_WAVEFRONT_GRAPH = 3  /* the same kernels over resident grids, reading their queue sizes
@@ -362,6 +362,27 @@ typedef struct lgpu_view_desc {
  * `stream`; the call returns when every film is complete. */
 LGPU_API int lgpu_render_batch(lgpu_context *ctx, const lgpu_view_desc *views, int32_t n_views,
                                const lgpu_render_opts *opts, void *stream);
+
+/* Result of lgpu_autotune: the execution scheme chosen for a workload. */
+typedef struct lgpu_tuning {
+    int32_t kernel_mode;      /* LGPU_KERNEL_MEGAKERNEL, _WAVEFRONT or _WAVEFRONT_GRAPH */
+    int32_t pool_slots;       /* wavefront path-slot pool */
+    int32_t block_size;       /* trace-kernel threads per block */
+    int32_t pad;
+    double mpaths_per_s;      /* throughput of the chosen scheme on the probe */
+    int32_t tried;            /* candidate schemes timed */
+    int32_t pad2;
+} lgpu_tuning;
+
+/* Autotuner (no counterpart in the reference): times the candidate schemes -- megakernel,
+ * host-driven wavefront and graph-replayed wavefront, path-slot pools of 2^18, 2^20 and 2^22, trace
+ * blocks of 64 to 512 threads -- on a probe of the given views rendered at min(spp, probe_spp)
+ * samples per pixel into scratch films (the views' own films are not touched), keeps the fastest in
+ * the context for every later render with kernel_mode AUTO (explicit pool_slots / block_size in
+ * those opts still win) and writes it to *out.  Allocates its scratch films for the duration of
+ * the call. */
+LGPU_API int lgpu_autotune(lgpu_context *ctx, const lgpu_view_desc *views, int32_t n_views,
+                           const lgpu_render_opts *opts, int32_t probe_spp, lgpu_tuning *out);
 
 /* Fixed-scratch variant of lgpu_render_paths, for callers that must not allocate.
  * No counterpart in the reference, which renders on the CPU.

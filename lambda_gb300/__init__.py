@@ -17,7 +17,7 @@ LIB_PATH = HERE / "_build" / "liblambda_gpu.so"
 
 EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_scene_commit", "lgpu_render",
            "lgpu_render_device", "lgpu_render_paths", "lgpu_render_count", "lgpu_intersect",
-           "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc", "lgpu_render_batch"]
+           "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc", "lgpu_render_batch", "lgpu_autotune"]
 
 _lib = None
 
@@ -56,6 +56,8 @@ def lib():
         L.lgpu_version.restype = C.c_char_p
         L.lgpu_scene_check.argtypes = [C.POINTER(abi.SceneDesc), C.c_char_p, C.c_size_t]
         L.lgpu_render_batch.argtypes = [vp, C.POINTER(abi.ViewDesc), C.c_int32, C.POINTER(abi.RenderOpts), vp]
+        L.lgpu_autotune.argtypes = [vp, C.POINTER(abi.ViewDesc), C.c_int32, C.POINTER(abi.RenderOpts), C.c_int32,
+                                    C.POINTER(abi.Tuning)]
         _lib = L
     return _lib
 
@@ -127,13 +129,25 @@ class Renderer:
     def render_batch(self, views, opts, stream=None):
         """Batched render (lgpu_render_batch).  views: list of (camera, width, height, spp,
         max_bounces, seed, film_ptr) with film_ptr a device address of width*height float4."""
+        arr = self._views(views)
+        self._check(lib().lgpu_render_batch(self._h, arr, len(views), C.byref(opts),
+                                            C.c_void_p(stream) if stream else None))
+
+    @staticmethod
+    def _views(views):
         arr = (abi.ViewDesc * len(views))()
         for i, (cam, w, h, spp, depth, seed, film_ptr) in enumerate(views):
             arr[i].camera = cam.desc()
             arr[i].width, arr[i].height, arr[i].spp, arr[i].max_bounces = w, h, spp, depth
             arr[i].seed, arr[i].sample_offset, arr[i].film_dev = seed, 0, film_ptr
-        self._check(lib().lgpu_render_batch(self._h, arr, len(views), C.byref(opts),
-                                            C.c_void_p(stream) if stream else None))
+        return arr
+
+    def autotune(self, views, opts, probe_spp=1):
+        """lgpu_autotune over views (same tuple form as render_batch; film pointers unused)."""
+        t = abi.Tuning()
+        arr = self._views([v[:6] + (v[6] if len(v) > 6 else None,) for v in views])
+        self._check(lib().lgpu_autotune(self._h, arr, len(views), C.byref(opts), probe_spp, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in abi.Tuning._fields_ if not f.startswith("pad")}
 
     def render_count(self, camera, opts):
         cam = camera.desc()

@@ -80,6 +80,11 @@ class ViewDesc(C.Structure):
                 ("film_dev", C.c_void_p)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("kernel_mode", C.c_int32), ("pool_slots", C.c_int32), ("block_size", C.c_int32), ("pad", C.c_int32),
+                ("mpaths_per_s", C.c_double), ("tried", C.c_int32), ("pad2", C.c_int32)]
+
+
 class RenderOpts(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
                 ("max_bounces", C.c_int32), ("min_bounces", C.c_int32), ("integrator", C.c_int32),

@@ -40,6 +40,8 @@ struct lgpu_context {
     DeviceScene S;
     bool have_scene = false;
     lgpu_stats stats;
+    bool tuned = false;         /* lgpu_autotune result, used by kernel_mode AUTO */
+    lgpu_tuning tuning;
     unsigned long long *d_counters = nullptr;
     float4 *d_film = nullptr;
     size_t film_px = 0;
@@ -1129,8 +1131,22 @@ int wavefront_frame(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_ren
     return LGPU_OK;
 }
 
-int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o, float4 *film, float4 *paths,
+/* kernel_mode AUTO after lgpu_autotune: the tuned scheme, pool and block size (explicit values in
+ * opts win). */
+lgpu_render_opts effective_opts(const lgpu_context *c, const lgpu_render_opts *o) {
+    lgpu_render_opts r = *o;
+    if (r.kernel_mode == LGPU_KERNEL_AUTO && c->tuned) {
+        r.kernel_mode = c->tuning.kernel_mode;
+        if (r.pool_slots <= 0) r.pool_slots = c->tuning.pool_slots;
+        if (r.block_size <= 0) r.block_size = c->tuning.block_size;
+    }
+    return r;
+}
+
+int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o_in, float4 *film, float4 *paths,
                 const uint64_t *ids, uint64_t n, bool count, cudaStream_t s) {
+    const lgpu_render_opts eff = effective_opts(c, o_in);
+    const lgpu_render_opts *o = &eff;
     c->stats.trace_ms = c->stats.shade_ms = c->stats.spawn_ms = 0;
     c->stats.iterations = 0;
     for (int k = 0; k < 6; ++k) { c->stats.stage_ms[k] = 0; c->stats.resumed[k] = 0; }
@@ -1351,9 +1367,11 @@ int batch_chunk(lgpu_context *c, const lgpu_view_desc *views, int v0, int v1, co
 
 extern "C" {
 
-LGPU_API int lgpu_render_batch(lgpu_context *c, const lgpu_view_desc *views, int32_t n_views, const lgpu_render_opts *o,
+LGPU_API int lgpu_render_batch(lgpu_context *c, const lgpu_view_desc *views, int32_t n_views, const lgpu_render_opts *o_in,
                                void *stream) {
-    if (!c || !o || n_views < 0 || (n_views > 0 && !views)) return LGPU_ERR_INVALID_ARG;
+    if (!c || !o_in || n_views < 0 || (n_views > 0 && !views)) return LGPU_ERR_INVALID_ARG;
+    const lgpu_render_opts eff = effective_opts(c, o_in);
+    const lgpu_render_opts *o = &eff;
     if (!c->have_scene) return fail(c, LGPU_ERR_NO_SCENE, "no committed scene");
     if (o->integrator != LGPU_INTEGRATOR_GPU_MISVOLPATH && o->integrator != LGPU_INTEGRATOR_VOLPATH)
         return fail(c, LGPU_ERR_INVALID_ARG, "integrator not available on the GPU path");
@@ -1420,6 +1438,73 @@ LGPU_API int lgpu_render_batch(lgpu_context *c, const lgpu_view_desc *views, int
     cudaEventRecord(c->ev1, st);
     c->stats.paths = all;
     return finish_timing(c);
+}
+
+}  // extern "C"
+
+/* ------------------------------------------------------------------ autotuner
+ *
+ * lgpu_autotune times candidate execution schemes on a probe of the caller's workload (the same
+ * views at a reduced spp, into scratch films) and keeps the fastest in the context, where
+ * kernel_mode AUTO picks it up: megakernel, host-driven wavefront or graph-replayed wavefront,
+ * path-slot pool 2^18 .. 2^22, trace block 64 .. 512 threads. */
+extern "C" {
+
+LGPU_API int lgpu_autotune(lgpu_context *c, const lgpu_view_desc *views, int32_t n_views, const lgpu_render_opts *o,
+                           int32_t probe_spp, lgpu_tuning *out) {
+    if (!c || !o || !views || n_views <= 0 || !out) return LGPU_ERR_INVALID_ARG;
+    if (!c->have_scene) return fail(c, LGPU_ERR_NO_SCENE, "no committed scene");
+    cudaSetDevice(c->device);
+    const int ps = probe_spp > 0 ? probe_spp : 1;
+    std::vector<lgpu_view_desc> probe(views, views + n_views);
+    uint64_t px = 0, paths = 0;
+    for (auto &v : probe) {
+        if (v.width <= 0 || v.height <= 0 || v.spp <= 0) return fail(c, LGPU_ERR_INVALID_ARG, "view width, height and spp must be positive");
+        v.spp = std::min(v.spp, ps);
+        px += (uint64_t)v.width * v.height;
+        paths += (uint64_t)v.width * v.height * v.spp;
+    }
+    float4 *scratch = nullptr;
+    cudaError_t e = cudaMalloc(&scratch, px * sizeof(float4));
+    if (e != cudaSuccess) return cuda_fail(c, e, "autotune films");
+    uint64_t off = 0;
+    for (auto &v : probe) { v.film_dev = reinterpret_cast<float *>(scratch + off); off += (uint64_t)v.width * v.height; }
+    struct Cand { int mode, pool, block; };
+    std::vector<Cand> cands = {{LGPU_KERNEL_MEGAKERNEL, 0, 128}};
+    for (int mode : {LGPU_KERNEL_WAVEFRONT, LGPU_KERNEL_WAVEFRONT_GRAPH})
+        for (int pool : {1 << 18, 1 << 20, 1 << 22}) {
+            if ((uint64_t)pool > 2 * paths && pool != (1 << 18)) continue;   /* larger than the work: same as smaller */
+            for (int block : {64, 128, 256, 512}) cands.push_back({mode, pool, block});
+        }
+    const bool was_tuned = c->tuned;
+    c->tuned = false;
+    double best = 0;
+    Cand bc = cands[0];
+    int tried = 0, rc = LGPU_OK;
+    for (const Cand &k : cands) {
+        lgpu_render_opts t = *o;
+        t.kernel_mode = k.mode; t.pool_slots = k.pool; t.block_size = k.block;
+        double ms = 0;
+        for (int rep = 0; rep < 2 && rc == LGPU_OK; ++rep) {   /* warm-up, then the timed run */
+            rc = lgpu_render_batch(c, probe.data(), (int32_t)probe.size(), &t, nullptr);
+            ms = c->stats.last_render_ms;
+        }
+        if (rc) break;
+        ++tried;
+        const double mps = (double)paths / (ms * 1e-3) / 1e6;
+        if (mps > best) { best = mps; bc = k; }
+    }
+    cudaFree(scratch);
+    if (rc) { c->tuned = was_tuned; return rc; }
+    c->tuning.kernel_mode = bc.mode;
+    c->tuning.pool_slots = bc.pool;
+    c->tuning.block_size = bc.block;
+    c->tuning.pad = 0;
+    c->tuning.mpaths_per_s = best;
+    c->tuning.tried = tried;
+    c->tuned = true;
+    *out = c->tuning;
+    return LGPU_OK;
 }
 
 }  // extern "C"

@@ -90,3 +90,28 @@ def test_batch_rejects_bad_view(gpu_lib):
             r.render_batch([(Camera((0, 0, -3.4), (0, 0, 0)), 4, 4, 0, 4, 1, f.data_ptr())], opts)
     finally:
         r.close()
+
+
+def test_autotune_then_auto_mode(gpu_lib):
+    """The autotuner times its candidates on a probe and AUTO renders then use the winner; the
+    films still match the plain wavefront (exactly, or within the atomic-order tolerance when the
+    megakernel wins)."""
+    torch = pytest.importorskip("torch")
+    from lambda_gb300 import abi, configs
+    from lambda_gb300.scene import Camera
+    sb, _, opts = configs.cornell(16, 16, 1)
+    views = _views(Camera)[:3]
+    r = gpu_lib.Renderer(sb)
+    try:
+        t = r.autotune([v + (0,) for v in views], opts, probe_spp=1)
+        assert t["kernel_mode"] in (abi.KERNEL_MEGAKERNEL, abi.KERNEL_WAVEFRONT, abi.KERNEL_WAVEFRONT_GRAPH)
+        assert t["tried"] >= 5 and t["mpaths_per_s"] > 0
+        opts.kernel_mode = abi.KERNEL_AUTO
+        auto = _render_batch(torch, r, views, opts)
+        opts.kernel_mode = abi.KERNEL_WAVEFRONT
+        opts.pool_slots, opts.block_size = 0, 0
+        ref = _render_batch(torch, r, views, opts)
+        for a, b in zip(auto, ref):
+            np.testing.assert_allclose(a, b, rtol=1e-4, atol=1e-5)
+    finally:
+        r.close()
