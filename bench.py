@@ -62,6 +62,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--mode", default="auto", choices=["auto", "megakernel", "wavefront", "graph"])
     p.add_argument("--pool", type=int, default=0, help="wavefront path-slot pool size (0 = default)")
+    p.add_argument("--block", type=int, default=0, help="trace-kernel block size (0 = default)")
+    p.add_argument("--workload", default="terrain", choices=["terrain", "batched"],
+                   help="terrain: the 1080p many-light frame; batched: 64 uneven views of the terrain and "
+                        "volume scenes in one batched render against the same views one at a time")
     return p.parse_args()
 
 
@@ -205,8 +209,111 @@ def kernel_table(per_step, stats, paths, kernel_ms, megakernel):
     return k
 
 
+def batched_views(seed=6, n=64):
+    """64 seeded views over the terrain (scene 0) and volume (scene 1) scenes: resolution in
+    {128, 256, 512, 1024}^2, spp uniform in 1..64, depth uniform in 4..12, cameras orbiting each
+    scene's default viewpoint."""
+    from lambda_gb300.scene import Camera
+    rng = np.random.RandomState(seed)
+    out = []
+    for i in range(n):
+        scene = int(rng.randint(0, 2))
+        res = int(rng.choice([128, 256, 512, 1024]))
+        spp = int(rng.randint(1, 65))
+        depth = int(rng.randint(4, 13))
+        if scene == 0:
+            o = np.array([-30.0, 22.0, -38.0]) + rng.uniform(-12, 12, 3) * np.array([1, 0.3, 1])
+            cam = Camera(tuple(o), (5.0, -2.0, 5.0), fov=1.1)
+        else:
+            a = rng.uniform(-0.6, 0.6)
+            o = (60.0 * np.sin(a), 10.0 + rng.uniform(-4, 4), -60.0 * np.cos(a))
+            cam = Camera(o, (0.0, 2.0, 0.0), fov=0.9)
+        out.append((scene, cam, res, res, spp, depth, 100 + i))
+    return out
+
+
+def main_batched(args):
+    """Batched uneven workload: every view of each scene in one lgpu_render_batch call (after
+    lgpu_autotune on a 1-spp probe) against the same views rendered one at a time."""
+    import torch
+    import lambda_gb300 as lg
+    from lambda_gb300 import abi, configs
+    lg.build()
+    torch.cuda.set_device(0)
+    views = batched_views()
+    sbs = [configs.terrain(64, 64, 1, 6)[0], configs.volume(64, 64, 1, 12)[0]]
+    rs = [lg.Renderer(sb, device=0) for sb in sbs]
+    films = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for (_, _, w, h, _, _, _) in views]
+    paths = sum(w * h * spp for (_, _, w, h, spp, _, _) in views)
+    opts = abi.render_opts(64, 64, 1, 6)
+    per_scene = [[(c, w, h, spp, d, seed, f.data_ptr()) for (sc, c, w, h, spp, d, seed), f in zip(views, films) if sc == k]
+                 for k in range(2)]
+    tuning = [r.autotune(v, opts, probe_spp=1) for r, v in zip(rs, per_scene)]
+    opts.kernel_mode = abi.KERNEL_AUTO
+
+    def batched():
+        for r, v in zip(rs, per_scene):
+            r.render_batch(v, opts)
+
+    def plain():
+        o = abi.render_opts(64, 64, 1, 6)
+        o.kernel_mode = abi.KERNEL_WAVEFRONT
+        for (sc, c, w, h, spp, d, seed), f in zip(views, films):
+            o.width, o.height, o.spp, o.max_bounces, o.seed = w, h, spp, d, seed
+            rs[sc].render_device(c, o, f.data_ptr())
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / args.steps
+
+    for f in films:
+        f.zero_()
+    clocks = ClockSampler(0)
+    clocks.start()
+    tb = timed(batched)
+    clk = clocks.stop()
+    counts_ok = all(bool(torch.all(f[..., 3] == float(spp * (max(1, args.warmup) + args.steps))))
+                    for f, (_, _, _, _, spp, _, _) in zip(films, views))
+    if not counts_ok:
+        raise SystemExit("work check failed: a view's film sample counts do not match its spp")
+    tp = timed(plain)
+    host = [torch.empty_like(f, device="cpu").pin_memory() for f in films]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batched()
+        for h_, f in zip(host, films):
+            h_.copy_(f, non_blocking=True)
+        torch.cuda.synchronize()
+    te = (time.perf_counter() - t0) / args.steps
+    cfg = {"workload": "batched uneven views: 64 views of the 1080p terrain and the volume/instancing scene, "
+                       "resolution in {128,256,512,1024}^2, spp 1-64, depth 4-12 (seed 6)",
+           "views": len(views), "path_samples": paths, "l2": "scene data and per-view films exceed L2",
+           "tuning": tuning}
+    line = {"metric": METRIC, "value": paths / tb / 1e6, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tb * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes and views)", "config": cfg,
+            "plain": {"value": paths / tp / 1e6, "ms_per_step": tp * 1e3,
+                      "scheme": "the same views one at a time through lgpu_render_device (wavefront)"},
+            "batched_over_plain": tp / tb,
+            "e2e": {"value": paths / te / 1e6, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(sum(f.numel() * 4 for f in films))},
+            "clocks": clk}
+    print(json.dumps(line))
+    for r in rs:
+        r.close()
+
+
 def main():
     args = parse()
+    if args.workload == "batched" and args.impl == "ours":
+        return main_batched(args)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -248,6 +355,7 @@ def main():
     opts.kernel_mode = {"auto": abi.KERNEL_AUTO, "megakernel": abi.KERNEL_MEGAKERNEL, "wavefront": abi.KERNEL_WAVEFRONT,
                         "graph": abi.KERNEL_WAVEFRONT_GRAPH}[args.mode]
     opts.pool_slots = args.pool
+    opts.block_size = args.block
     r = lg.Renderer(sb, device=dev)
     W, H, spp = opts.width, opts.height, opts.spp
     paths = W * H * spp

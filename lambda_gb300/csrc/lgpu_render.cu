@@ -302,8 +302,8 @@ size_t LG_CAT(wave_cold_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PCold<LGP
 
 #if LGPU_NS == 3
 /* Answer every queued query: closest hit (Scene::Intersect) or occlusion (rtcOccluded1). */
-template <bool COUNT>
-__global__ void __launch_bounds__(512) k_wave_trace(const __grid_constant__ WaveArgs W, int n) {
+template <bool COUNT, int BS>
+__global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveArgs W, int n) {
     LocalStack stk;   /* measured faster than a shared-memory column stack (L1 serves it) */
     int off[LG_NSEG + 1];
     if (W.count_in) {   /* device-driven: segment sizes from the device */
@@ -348,15 +348,22 @@ __global__ void __launch_bounds__(512) k_wave_trace(const __grid_constant__ Wave
 }
 /* n < 0: device-driven launch over a resident grid (the queue sizes are read on the device);
  * n == 0: set-up of the resident grid only.  block: 64, 128, 256 or 512 threads. */
-cudaError_t LG_CAT(wave_trace_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, cudaStream_t st, int block) {
-    const int bs = (block == 64 || block == 256 || block == 512) ? block : 128;
-    static int grid[4] = {0, 0, 0, 0};
-    const int gi = bs == 64 ? 0 : bs == 128 ? 1 : bs == 256 ? 2 : 3;
-    if (!grid[gi]) grid[gi] = resident_grid(k_wave_trace<LGPU_COUNT != 0>, bs, 0);
+template <int BS>
+static cudaError_t trace_launch(const WaveArgs &W, int n, cudaStream_t st) {
+    static int grid = 0;
+    if (!grid) grid = resident_grid(k_wave_trace<LGPU_COUNT != 0, BS>, BS, 0);   /* n == 0: set-up only */
     if (n == 0) return cudaSuccess;
-    const int blocks = n < 0 ? grid[gi] : (n + bs - 1) / bs;
-    k_wave_trace<LGPU_COUNT != 0><<<blocks, bs, 0, st>>>(W, n < 0 ? 0 : n);
+    const int blocks = n < 0 ? grid : (n + BS - 1) / BS;
+    k_wave_trace<LGPU_COUNT != 0, BS><<<blocks, BS, 0, st>>>(W, n < 0 ? 0 : n);
     return cudaGetLastError();
+}
+cudaError_t LG_CAT(wave_trace_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, cudaStream_t st, int block) {
+    switch (block) {
+    case 64: return trace_launch<64>(W, n, st);
+    case 256: return trace_launch<256>(W, n, st);
+    case 512: return trace_launch<512>(W, n, st);
+    default: return trace_launch<128>(W, n, st);
+    }
 }
 #endif
 
