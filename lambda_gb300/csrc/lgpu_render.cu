@@ -183,17 +183,18 @@ __device__ __forceinline__ void warp_stage(PHot<NS> *G, PHot<NS> *sh, int slot, 
  * a launch sized to the queue runs the loop body once per thread; a device-driven launch (fixed
  * grid, n read from W.count_in) loops.  The loop bound is block-uniform, so warps stay converged
  * for the warp-cooperative staging. */
-template <int NS, bool COUNT>
+template <int NS, bool COUNT, bool DEV>
 __global__ void __launch_bounds__(128) k_wave_resume(const __grid_constant__ WaveArgs W, int n) {
     extern __shared__ float4 smem4[];
-    if (W.count_in) n = W.count_in[W.seg_sel];
+    if (DEV) n = W.count_in[W.seg_sel];
     PHot<NS> *G = reinterpret_cast<PHot<NS> *>(W.states);
     PHot<NS> *sh = reinterpret_cast<PHot<NS> *>(smem4) + (threadIdx.x & ~31);
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const int step = DEV ? gridDim.x * blockDim.x : n;   /* host-sized launches run the body once */
+    for (int base = blockIdx.x * blockDim.x; base < n; base += step) {
         const int i = base + threadIdx.x;
         int slot = -1;
         if (i < n) {
-            if (W.count_in) {
+            if (DEV) {
                 slot = W.queue_in[W.seg_sel * W.cap + i];
             } else {
                 int seg = 0;
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(128) k_wave_resume(const __grid_constant__ Wav
 /* Start new paths in free slots: consecutive path ids go to consecutive free-list entries, so the
  * warps of a spawn trace neighbouring samples of one pixel.  Slots come from the free list, or from
  * the untouched tail of the pool on the first spawn.  Grid-stride like k_wave_resume. */
-template <int NS, bool COUNT>
+template <int NS, bool COUNT, bool DEV>
 __global__ void __launch_bounds__(128) k_wave_spawn(const __grid_constant__ WaveArgs W, int n_max, int fresh) {
     extern __shared__ float4 smem4[];
     const int nfree = fresh ? n_max : *W.free_count;
@@ -233,7 +234,8 @@ __global__ void __launch_bounds__(128) k_wave_spawn(const __grid_constant__ Wave
     const int m = (int)(nfree < (int)min(left, (unsigned long long)0x7fffffff) ? nfree : (int)left);
     PHot<NS> *G = reinterpret_cast<PHot<NS> *>(W.states);
     PHot<NS> *sh = reinterpret_cast<PHot<NS> *>(smem4) + (threadIdx.x & ~31);
-    for (int base = blockIdx.x * blockDim.x; base < m; base += gridDim.x * blockDim.x) {
+    const int step = DEV ? gridDim.x * blockDim.x : m;   /* host-sized launches run the body once */
+    for (int base = blockIdx.x * blockDim.x; base < m; base += step) {
         const int i = base + threadIdx.x;
         int keep = -1;
         if (i < m) {
@@ -271,30 +273,31 @@ static int resident_grid(K kernel, int block, size_t smem) {
 }
 
 cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, int start_new, cudaStream_t st) {
+    constexpr bool C = LGPU_COUNT != 0;
     const size_t smem = 128 * sizeof(PHot<LGPU_NS>);
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_wave_resume<LGPU_NS, LGPU_COUNT != 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_wave_spawn<LGPU_NS, LGPU_COUNT != 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        configured = true;
-    }
     static int grid_resume = 0, grid_spawn = 0;
     if (!grid_resume) {
-        grid_resume = resident_grid(k_wave_resume<LGPU_NS, LGPU_COUNT != 0>, 128, smem);
-        grid_spawn = resident_grid(k_wave_spawn<LGPU_NS, LGPU_COUNT != 0>, 128, smem);
+        for (auto k : {k_wave_resume<LGPU_NS, C, false>, k_wave_resume<LGPU_NS, C, true>})
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        for (auto k : {k_wave_spawn<LGPU_NS, C, false>, k_wave_spawn<LGPU_NS, C, true>})
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        grid_resume = resident_grid(k_wave_resume<LGPU_NS, C, true>, 128, smem);
+        grid_spawn = resident_grid(k_wave_spawn<LGPU_NS, C, true>, 128, smem);
     }
     /* n < 0: device-driven launch over a fixed resident grid (sizes read on the device) */
     if (start_new) {
         /* spawn into up to |n| slots (fresh pool or free list), then advance the path counter */
         const int nm = n < 0 ? -n : n;
-        const int blocks = n < 0 ? std::min(grid_spawn, (nm + 127) / 128) : (n + 127) / 128;
-        if (nm > 0) k_wave_spawn<LGPU_NS, LGPU_COUNT != 0><<<blocks, 128, smem, st>>>(W, nm, start_new == 2);
+        if (nm > 0) {
+            if (n < 0) k_wave_spawn<LGPU_NS, C, true><<<std::min(grid_spawn, (nm + 127) / 128), 128, smem, st>>>(W, nm, start_new == 2);
+            else k_wave_spawn<LGPU_NS, C, false><<<(nm + 127) / 128, 128, smem, st>>>(W, nm, start_new == 2);
+        }
         k_wave_advance<<<1, 1, 0, st>>>(W, nm, start_new == 2);
         return cudaGetLastError();
     }
     if (n == 0) return cudaSuccess;
-    const int blocks = n < 0 ? grid_resume : (n + 127) / 128;
-    k_wave_resume<LGPU_NS, LGPU_COUNT != 0><<<blocks, 128, smem, st>>>(W, n < 0 ? 0 : n);
+    if (n < 0) k_wave_resume<LGPU_NS, C, true><<<grid_resume, 128, smem, st>>>(W, 0);
+    else k_wave_resume<LGPU_NS, C, false><<<(n + 127) / 128, 128, smem, st>>>(W, n);
     return cudaGetLastError();
 }
 size_t LG_CAT(wave_state_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PHot<LGPU_NS>); }
@@ -302,11 +305,11 @@ size_t LG_CAT(wave_cold_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PCold<LGP
 
 #if LGPU_NS == 3
 /* Answer every queued query: closest hit (Scene::Intersect) or occlusion (rtcOccluded1). */
-template <bool COUNT, int BS>
+template <bool COUNT, int BS, bool DEV>
 __global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveArgs W, int n) {
     LocalStack stk;   /* measured faster than a shared-memory column stack (L1 serves it) */
     int off[LG_NSEG + 1];
-    if (W.count_in) {   /* device-driven: segment sizes from the device */
+    if (DEV) {   /* device-driven: segment sizes from the device */
         off[0] = 0;
 #pragma unroll
         for (int k = 0; k < LG_NSEG; ++k) off[k + 1] = off[k] + W.count_in[k];
@@ -315,9 +318,10 @@ __global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveA
 #pragma unroll
         for (int k = 0; k <= LG_NSEG; ++k) off[k] = W.seg_off[k];
     }
-    const int stride = W.count_in ? W.cap : W.cap_in;
+    const int stride = DEV ? W.cap : W.cap_in;
     TravStats st = {0u, 0u, 0u};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int step = DEV ? gridDim.x * blockDim.x : n;   /* host-sized launches run the body once */
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
         int seg = 0, first = 0;
 #pragma unroll
         for (int k = 1; k < LG_NSEG; ++k) seg += (i >= off[k]) ? 1 : 0;
@@ -351,10 +355,10 @@ __global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveA
 template <int BS>
 static cudaError_t trace_launch(const WaveArgs &W, int n, cudaStream_t st) {
     static int grid = 0;
-    if (!grid) grid = resident_grid(k_wave_trace<LGPU_COUNT != 0, BS>, BS, 0);   /* n == 0: set-up only */
+    if (!grid) grid = resident_grid(k_wave_trace<LGPU_COUNT != 0, BS, true>, BS, 0);   /* n == 0: set-up only */
     if (n == 0) return cudaSuccess;
-    const int blocks = n < 0 ? grid : (n + BS - 1) / BS;
-    k_wave_trace<LGPU_COUNT != 0, BS><<<blocks, BS, 0, st>>>(W, n < 0 ? 0 : n);
+    if (n < 0) k_wave_trace<LGPU_COUNT != 0, BS, true><<<grid, BS, 0, st>>>(W, 0);
+    else k_wave_trace<LGPU_COUNT != 0, BS, false><<<(n + BS - 1) / BS, BS, 0, st>>>(W, n);
     return cudaGetLastError();
 }
 cudaError_t LG_CAT(wave_trace_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, cudaStream_t st, int block) {
