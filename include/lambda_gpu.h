@@ -213,6 +213,14 @@ typedef struct lgpu_medium_desc {
     float pad;
 } lgpu_medium_desc;
 
+/* Image texture (texture_t<Colour>, src/image/Texture.h): width * height RGBA float texels in
+ * scanline-row order (texel (x, y) at (y * width + x) * 4), sampled by IMAGE_TEXTURE nodes
+ * (params[0] = texture index) with GetPixelUVBilinear at fract(uv). */
+typedef struct lgpu_texture_desc {
+    const float *rgba;
+    int32_t width, height;
+} lgpu_texture_desc;
+
 typedef struct lgpu_scene_desc {
     const lgpu_mesh_desc *meshes;       int32_t num_meshes;
     const lgpu_object_desc *objects;    int32_t num_objects;
@@ -222,6 +230,7 @@ typedef struct lgpu_scene_desc {
     const lgpu_medium_desc *media;      int32_t num_media;
     int32_t has_volumes;      /* Scene::hasVolumes (src/core/Scene.h:36) */
     int32_t light_strategy;   /* lgpu_light_strategy */
+    const lgpu_texture_desc *textures; int32_t num_textures;
 } lgpu_scene_desc;
 
 /* Pinhole camera (src/camera/Camera.cpp:7-44): origin, the three axes and the field of view.

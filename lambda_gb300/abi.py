@@ -59,6 +59,10 @@ class MediumDesc(C.Structure):
     _fields_ = [("sigma_a", C.c_float * 3), ("sigma_s", C.c_float * 3), ("g", C.c_float), ("pad", C.c_float)]
 
 
+class TextureDesc(C.Structure):
+    _fields_ = [("rgba", F32P), ("width", C.c_int32), ("height", C.c_int32)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("meshes", C.POINTER(MeshDesc)), ("num_meshes", C.c_int32),
                 ("objects", C.POINTER(ObjectDesc)), ("num_objects", C.c_int32),
@@ -66,7 +70,8 @@ class SceneDesc(C.Structure):
                 ("nodes", C.POINTER(NodeDesc)), ("num_nodes", C.c_int32),
                 ("lights", C.POINTER(LightDesc)), ("num_lights", C.c_int32),
                 ("media", C.POINTER(MediumDesc)), ("num_media", C.c_int32),
-                ("has_volumes", C.c_int32), ("light_strategy", C.c_int32)]
+                ("has_volumes", C.c_int32), ("light_strategy", C.c_int32),
+                ("textures", C.POINTER(TextureDesc)), ("num_textures", C.c_int32)]
 
 
 class CameraDesc(C.Structure):

@@ -172,6 +172,75 @@ def cornell(width=256, height=256, spp=16, max_depth=8, subdiv=3, light_intensit
     return sb, cam, opts
 
 
+# ------------------------------------------------------------------ config: inverse rendering
+def inverse_cameras(n=8, radius=3.0, spread=0.6):
+    """n pinhole cameras on an arc of the ring of the given radius around the box centre, facing
+    the open side of the box (a full ring would see the outside of the walls)."""
+    cams = []
+    for k in range(n):
+        a = -spread + 2 * spread * k / max(1, n - 1)
+        cams.append(Camera((radius * np.sin(a), 0.15 * np.cos(3 * a), -radius * np.cos(a)), (0, 0, 0), fov=0.8))
+    return cams
+
+
+def cornell_inverse(width=512, height=512, spp=4, max_depth=8, albedo=None, roughness=0.3, sigma_a=0.1,
+                    sigma_s=0.8, tex_res=64, seed=5):
+    """Cornell box whose back wall albedo is a tex_res^2 image texture, whose sphere is GGX with a
+    scalar roughness, and which holds a homogeneous-medium cube of side 0.4 (null surface).  The
+    unknowns of the inverse-rendering workload are that texture, the roughness and the cube's
+    sigma_a / sigma_s.  albedo: (tex_res, tex_res, 3) array, default seeded uniform [0.1, 0.9]."""
+    rng = np.random.RandomState(seed)
+    if albedo is None:
+        albedo = rng.uniform(0.1, 0.9, (tex_res, tex_res, 3)).astype(np.float32)
+    sb = SceneBuilder()
+    sb.has_volumes = True
+    tex = sb.texture(albedo)
+    img = sb.node("IMAGE_TEXTURE", [tex])
+    back = sb.node("BXDF_LAMBERTIAN", inputs={0: out(img, 0)})
+    white = sb.node("BXDF_LAMBERTIAN", inputs={0: (0.73, 0.73, 0.73, 1)})
+    red = sb.node("BXDF_LAMBERTIAN", inputs={0: (0.65, 0.05, 0.05, 1)})
+    green = sb.node("BXDF_LAMBERTIAN", inputs={0: (0.05, 0.65, 0.05, 1)})
+    black = sb.node("BXDF_LAMBERTIAN", inputs={0: (0.0, 0.0, 0.0, 1)})
+    ggx = sb.node("BXDF_MICROFACET_R", [abi.DIST_TROWBRIDGE_REITZ, 1.5], {0: (0.9, 0.9, 0.9, 1), 1: float(roughness)})
+    m_back, m_white, m_red, m_green, m_ggx = (sb.material(b) for b in (back, white, red, green, ggx))
+    walls = [((-1, -1, -1), (-1, -1, 1), (1, -1, 1), (1, -1, -1), m_white),
+             ((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1), m_white),
+             ((-1, -1, 1), (-1, 1, 1), (1, 1, 1), (1, -1, 1), m_back),
+             ((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1), m_red),
+             ((1, -1, -1), (1, -1, 1), (1, 1, 1), (1, 1, -1), m_green)]
+    for p0, p1, p2, p3, m in walls:
+        v, t = quad(p0, p1, p2, p3)
+        sb.obj(sb.mesh(v, t, uvs=[(0, 0), (0, 1), (1, 1), (1, 0)]), m)
+    sv, st = icosphere(3, 0.3, (0.35, -0.7, 0.25))
+    sb.obj(sb.mesh(sv, st), m_ggx)
+    med = sb.medium(float(sigma_a), float(sigma_s), 0.0)
+    m_box = sb.material(-1, medium_interior=med)
+    c, hs = np.array([-0.4, -0.6, -0.1]), 0.2
+    for p0, p1, p2, p3 in box_faces(c, hs):
+        v, t = quad(p0, p1, p2, p3)
+        sb.obj(sb.mesh(v, t), m_box)
+    h = 0.125
+    lv, lt = quad((-h, 0.999, -h), (h, 0.999, -h), (h, 0.999, h), (-h, 0.999, h))
+    emis = blackbody_emission(sb, 6500.0)
+    m_light = sb.material(black, light=len(sb.lights))
+    lobj = sb.obj(sb.mesh(lv, lt), m_light)
+    sb.light_mesh(lobj, emis, 40.0)
+    opts = abi.render_opts(width, height, spp, max_depth)
+    return sb, inverse_cameras(), opts
+
+
+def box_faces(c, hs):
+    """Six outward-facing quads of an axis-aligned cube (centre c, half side hs)."""
+    x0, y0, z0 = c - hs
+    x1, y1, z1 = c + hs
+    return [((x0, y0, z0), (x1, y0, z0), (x1, y0, z1), (x0, y0, z1)),
+            ((x0, y1, z0), (x0, y1, z1), (x1, y1, z1), (x1, y1, z0)),
+            ((x0, y0, z0), (x0, y1, z0), (x1, y1, z0), (x1, y0, z0)),
+            ((x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1)),
+            ((x0, y0, z0), (x0, y0, z1), (x0, y1, z1), (x0, y1, z0)),
+            ((x1, y0, z0), (x1, y1, z0), (x1, y1, z1), (x1, y0, z1))]
+
+
 # ------------------------------------------------------------------ config: many-light terrain
 def sky_texture(w=512, h=256):
     v = (np.arange(h) + 0.5) / h

@@ -194,6 +194,10 @@ bool check_prog(const HostScene &H, int off, int len, std::string &why) {
         if (in.op >= OP_COUNT) { why = "bad opcode"; return false; }
         if (in.dst >= LGPU_MAX_REGS || in.a >= LGPU_MAX_REGS || in.b >= LGPU_MAX_REGS || in.c >= LGPU_MAX_REGS) { why = "register index"; return false; }
         if (in.op == OP_MERGE && in.sub != 255 && in.sub >= LGPU_MAX_REGS) { why = "merge register"; return false; }
+        if (in.op == OP_IMAGE) {
+            const int off = float_to_bits(in.k[0]), w = (int)in.k[1], h = (int)in.k[2];
+            if (off < 0 || w <= 0 || h <= 0 || (size_t)off + (size_t)w * h > H.envTex.size()) { why = "image texture range"; return false; }
+        }
     }
     return true;
 }
@@ -545,9 +549,19 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
 
     /* ---------------- materials */
     std::vector<DIns> &code = H.code;
+    /* image textures first: their texels share the float4 pool of the environment map */
+    std::vector<int> texOff;
+    for (int t = 0; t < d->num_textures; ++t) {
+        const lgpu_texture_desc &td = d->textures[t];
+        if (!td.rgba || td.width <= 0 || td.height <= 0) return fail(c, LGPU_ERR_INVALID_SCENE, "image texture without texels");
+        texOff.push_back((int)H.envTex.size());
+        for (int k = 0; k < td.width * td.height; ++k)
+            H.envTex.push_back(make_float4(td.rgba[4 * k], td.rgba[4 * k + 1], td.rgba[4 * k + 2], td.rgba[4 * k + 3]));
+    }
     GraphCompiler gc;
     gc.d = d;
     gc.code = &code;
+    gc.tex_off = &texOff;
     std::vector<DMaterial> &mats = H.mats;
     mats.resize(d->num_materials);
     for (int i = 0; i < d->num_materials; ++i) {
@@ -615,6 +629,7 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
                         ShadeCtx sc;
                         std::memset(&sc, 0, sizeof(sc));
                         sc.eta = 1.001f;
+                        sc.texels = H.envTex.data();
                         if (m.uvs) {
                             const float *u0 = m.uvs + 2 * m.triangles[3 * t], *u1 = m.uvs + 2 * m.triangles[3 * t + 1], *u2 = m.uvs + 2 * m.triangles[3 * t + 2];
                             const float fu = (float)aa * inv3, fv = (float)bb * inv3;

@@ -29,6 +29,7 @@ void build_bvh(const std::vector<Aabb> &boxes, int max_leaf, int node_base, int 
 struct GraphCompiler {
     const lgpu_scene_desc *d = nullptr;
     std::vector<DIns> *code = nullptr;
+    const std::vector<int> *tex_off = nullptr;   /* texel-pool offset of each scene texture */
     std::string err;
     /* compile the BSDF of a material into m (program appended to *code) */
     bool compile_material(int bxdf_node, DMaterial &m);

@@ -178,6 +178,7 @@ struct Val { int vreg; uint8_t type; };
 
 struct Emitter {
     const lgpu_scene_desc *d;
+    const std::vector<int> *tex_off = nullptr;
     std::vector<DIns> ins;          /* SSA: instruction i writes virtual register i */
     std::map<std::pair<int, int>, Val> memo;
     std::string err;
@@ -288,6 +289,17 @@ struct Emitter {
         case LGPU_NODE_RGB: r = konst(nd.params[0], nd.params[1], nd.params[2], 1.f); break;
         case LGPU_NODE_SPECTRUM: r = conv(konst(nd.params[0], nd.params[1], nd.params[2], 1.f), ST_COLOUR, ST_SPECTRUM, false); break;
         case LGPU_NODE_SURFACE_INFO: r = emit(mkins(OP_NORMAL)); break;
+        case LGPU_NODE_IMAGE_TEXTURE: {
+            const int ti = (int)nd.params[0];
+            if (!tex_off || ti < 0 || ti >= d->num_textures || ti >= (int)tex_off->size()) { err = "image texture node without a scene texture"; break; }
+            DIns in = mkins(OP_IMAGE);
+            in.sub = (uint8_t)(out == 1 ? 1 : 0);
+            in.k[0] = bits_to_float((*tex_off)[ti]);
+            in.k[1] = (float)d->textures[ti].width;
+            in.k[2] = (float)d->textures[ti].height;
+            r = emit(in);
+            break;
+        }
         case LGPU_NODE_BLACKBODY: {
             const int samples = nd.params[0] > 0 ? (int)nd.params[0] : 3;
             const int src = nd.in_node[0];
@@ -438,6 +450,7 @@ struct Emitter {
 bool GraphCompiler::compile_material(int bxdf_node, DMaterial &m) {
     Emitter E;
     E.d = d;
+    E.tex_off = tex_off;
     m.num_leaves = 0;
     m.num_tree = 0;
     struct LeafV { int alb, rough; };
@@ -521,7 +534,7 @@ bool GraphCompiler::compile_material(int bxdf_node, DMaterial &m) {
 bool GraphCompiler::context_free(int off, int len) const {
     for (int i = 0; i < len; ++i) {
         const uint8_t op = (*code)[off + i].op;
-        if (op == OP_UV || op == OP_POINT || op == OP_NORMAL || op == OP_NOISE || op == OP_SCHLICK) return false;
+        if (op == OP_UV || op == OP_POINT || op == OP_NORMAL || op == OP_NOISE || op == OP_SCHLICK || op == OP_IMAGE) return false;
     }
     return true;
 }
@@ -546,6 +559,7 @@ void GraphCompiler::fold_material(DMaterial &m) {
 bool GraphCompiler::compile_emission(int node, int socket, int &prog_off, int &prog_len, int &out_reg) {
     Emitter E;
     E.d = d;
+    E.tex_off = tex_off;
     const Val v = E.output(node, socket);
     if (v.vreg < 0 || !E.err.empty()) { err = E.err.empty() ? "bad emission socket" : E.err; return false; }
     const int illum = E.spectrum_of(v, true);

@@ -21,7 +21,7 @@ namespace lg {
 /* ------------------------------------------------------------------ bytecode */
 enum Op : uint8_t {
     OP_CONST = 0, OP_UV, OP_POINT, OP_NORMAL, OP_NOISE, OP_MATHS, OP_VMATHS, OP_DOT, OP_CROSS, OP_LEN,
-    OP_CONV, OP_BBCONST, OP_BB, OP_SEP, OP_MERGE, OP_SCHLICK, OP_COUNT
+    OP_CONV, OP_BBCONST, OP_BB, OP_SEP, OP_MERGE, OP_SCHLICK, OP_IMAGE, OP_COUNT
 };
 /* socket value types (ShaderGraph.h:46-54) */
 enum SockT : uint8_t { ST_NULL = 0, ST_SCALAR, ST_COLOUR, ST_VEC2, ST_VEC3, ST_SPECTRUM, ST_BXDF };
@@ -35,7 +35,33 @@ struct ShadeCtx {
     float woLy;
     float eta;
     bool mediumInteraction;
+    const float4 *texels;   /* texel pool of IMAGE_TEXTURE nodes */
 };
+
+/* texture_t::GetPixelUVBilinear (src/image/Texture.h:71-81) at fract(uv)
+ * (ImageTextureInput::GetColour, src/shading/graph/GraphInputs.cpp:128-131); texel (x, y) at
+ * off + y * w + x.  Returns the filtered texel; the four weights and the base texel index are
+ * written for callers that differentiate through the fetch. */
+HD float4 image_bilinear(const float4 *tex, int off, int w, int h, float2 uv, int *base = nullptr, float *wts = nullptr) {
+    const float u = uv.x - floorf(uv.x), v = uv.y - floorf(uv.y);
+    const float fx = fminf((float)(w - 1), fminf(fmaxf(u, 0.f), 1.f) * (float)w);
+    const float fy = fminf((float)(h - 1), fminf(fmaxf(v, 0.f), 1.f) * (float)h);
+    const int x = (int)fx, y = (int)fy;
+    const int x1 = x + 1 < w ? x + 1 : w - 1, y1 = y + 1 < h ? y + 1 : h - 1;
+    const float tx = fx - (float)x, ty = fy - (float)y;
+    const float4 p00 = tex[off + y * w + x], p10 = tex[off + y * w + x1];
+    const float4 p01 = tex[off + y1 * w + x], p11 = tex[off + y1 * w + x1];
+    const float4 ya = make_float4(p00.x + (p10.x - p00.x) * tx, p00.y + (p10.y - p00.y) * tx,
+                                  p00.z + (p10.z - p00.z) * tx, p00.w + (p10.w - p00.w) * tx);
+    const float4 yb = make_float4(p01.x + (p11.x - p01.x) * tx, p01.y + (p11.y - p01.y) * tx,
+                                  p01.z + (p11.z - p01.z) * tx, p01.w + (p11.w - p01.w) * tx);
+    if (base) {
+        base[0] = y * w + x; base[1] = y * w + x1; base[2] = y1 * w + x; base[3] = y1 * w + x1;
+        wts[0] = (1.f - tx) * (1.f - ty); wts[1] = tx * (1.f - ty); wts[2] = (1.f - tx) * ty; wts[3] = tx * ty;
+    }
+    return make_float4(ya.x + (yb.x - ya.x) * ty, ya.y + (yb.y - ya.y) * ty, ya.z + (yb.z - ya.z) * ty,
+                       ya.w + (yb.w - ya.w) * ty);
+}
 
 /* -------- spectral conversions -------- */
 HD float smits_at(const float *curve, float l) {
@@ -222,6 +248,11 @@ __host__ __device__ __noinline__ void run_prog(const DIns *p, int n, const Shade
         case OP_UV: r = make_float4(c.uv.x, c.uv.y, 0.f, 0.f); break;
         case OP_POINT: r = make_float4(c.point.x, c.point.y, c.point.z, 0.f); break;
         case OP_NORMAL: r = make_float4(c.normalS.x, c.normalS.y, c.normalS.z, 0.f); break;
+        case OP_IMAGE: {   /* k = (texel offset bits, width, height); sub 0 colour, 1 scalar (red) */
+            r = image_bilinear(c.texels, float_to_bits(in.k[0]), (int)in.k[1], (int)in.k[2], c.uv);
+            if (in.sub == 1) r = make_float4(r.x, 0.f, 0.f, 0.f);
+            break;
+        }
         case OP_NOISE: {
             float v = 0.f;
             if (in.sub == NK_OCTAVE) {   /* OctaveNoise::Get2D / Get3D (GraphTexture.cpp:157-175) */

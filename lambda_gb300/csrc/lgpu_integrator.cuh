@@ -90,6 +90,7 @@ struct Tracer {
         ShadeCtx c;
         c.point = h.point; c.normalS = h.nS; c.uv = h.uv; c.woLy = ev.woL.y; c.eta = ev.eta;
         c.mediumInteraction = ev.mediumInteraction;
+        c.texels = S.env_tex;
         run_prog<NS>(S.prog + L.prog_off, L.prog_len, c, lam, R);
         /* the program ends with a conversion to a spectrum; the reflectance variant sits one
          * register above the illuminant one */
@@ -456,6 +457,7 @@ struct Tracer {
         ShadeCtx c;
         c.point = h.point; c.normalS = h.nS; c.uv = h.uv; c.woLy = ev.woL.y; c.eta = ev.eta;
         c.mediumInteraction = ev.mediumInteraction;
+        c.texels = S.env_tex;
         run_prog<NS>(S.prog + m.prog_off, m.prog_len, c, lam, R);
         for (int i = 0; i < m.num_leaves; ++i) {
             b.alb[i] = Spec<NS>::from4(R[m.leaves[i].albedo]);

@@ -29,6 +29,11 @@ HD float bits_to_float(int v) {
     u.i = v;
     return u.f;
 }
+HD int float_to_bits(float f) {
+    union { float f; int i; } u;
+    u.f = f;
+    return u.i;
+}
 HD float finf() { return bits_to_float(0x7f800000); }
 HD float fmaxreal() { return 3.402823466e+38f; }
 /* std::max / std::min exactly: the first argument's NaN propagates. */

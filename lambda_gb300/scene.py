@@ -40,6 +40,7 @@ class SceneBuilder:
     def __init__(self):
         self.meshes, self.objects, self.materials = [], [], []
         self.nodes, self.lights, self.media = [], [], []
+        self.textures = []
         self.has_volumes = False
         self.light_strategy = abi.LIGHT_STRATEGY_TREE
         self._keep = []
@@ -135,6 +136,16 @@ class SceneBuilder:
         self.media.append((sa, ss, g))
         return len(self.media) - 1
 
+    def texture(self, rgba):
+        """Image texture (height, width, 4) float texels, row y then column x; returns its index
+        for an IMAGE_TEXTURE node's params[0]."""
+        t = np.ascontiguousarray(rgba, np.float32)
+        if t.ndim == 3 and t.shape[2] == 3:
+            t = np.ascontiguousarray(np.concatenate([t, np.ones(t.shape[:2] + (1,), np.float32)], 2))
+        assert t.ndim == 3 and t.shape[2] == 4
+        self.textures.append(t)
+        return len(self.textures) - 1
+
     # ---------------------------------------------------------------- descriptor
     def desc(self):
         ms = (abi.MeshDesc * max(1, len(self.meshes)))()
@@ -156,10 +167,13 @@ class SceneBuilder:
             media[i].sigma_a[:] = sa
             media[i].sigma_s[:] = ss
             media[i].g = g
+        texs = (abi.TextureDesc * max(1, len(self.textures)))()
+        for i, t in enumerate(self.textures):
+            texs[i].rgba, texs[i].height, texs[i].width = _fptr(t), t.shape[0], t.shape[1]
         d = abi.SceneDesc(ms, len(self.meshes), obs, len(self.objects), mats, len(self.materials),
                           nodes, len(self.nodes), lights, len(self.lights), media, len(self.media),
-                          int(self.has_volumes), int(self.light_strategy))
-        self._keep.extend([ms, obs, mats, nodes, lights, media])
+                          int(self.has_volumes), int(self.light_strategy), texs, len(self.textures))
+        self._keep.extend([ms, obs, mats, nodes, lights, media, texs])
         return d
 
     @property

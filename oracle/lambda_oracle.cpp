@@ -378,6 +378,8 @@ static Val EvalOutput(const Graph &g, int node, int out, const ScatterEvent &ev)
 
 struct Graph {
     std::vector<lgpu_node_desc> nodes;
+    std::vector<std::vector<float>> tex;   /* image textures: RGBA texels, scanline rows */
+    std::vector<int> texW, texH;
     static SockT OutType(int type, int out) {
         switch (type) {
         case LGPU_NODE_BXDF_MIX: case LGPU_NODE_BXDF_LAMBERTIAN: case LGPU_NODE_BXDF_OREN_NAYAR_R:
@@ -392,6 +394,7 @@ struct Graph {
         case LGPU_NODE_RGB: return T_COLOUR;
         case LGPU_NODE_SPECTRUM: case LGPU_NODE_BLACKBODY: return T_SPECTRUM;
         case LGPU_NODE_SURFACE_INFO: return T_VEC3;
+        case LGPU_NODE_IMAGE_TEXTURE: return out == 0 ? T_COLOUR : T_SCALAR;
         case LGPU_NODE_MATHS: case LGPU_NODE_DOT_PRODUCT: case LGPU_NODE_VECTOR_MAGNITUDE: return T_SCALAR;
         case LGPU_NODE_VECTOR_MATHS: case LGPU_NODE_CROSS_PRODUCT: return T_VEC3;
         case LGPU_NODE_PERLIN_NOISE: case LGPU_NODE_VALUE_NOISE: case LGPU_NODE_OCTAVE_NOISE:
@@ -595,6 +598,24 @@ static Val EvalOutput(const Graph &g, int node, int out, const ScatterEvent &ev)
     case LGPU_NODE_SPECTRUM: { const Real rgb[3] = {d.params[0], d.params[1], d.params[2]}; r.s = FromRGB(rgb, false); break; }
     case LGPU_NODE_BLACKBODY: r.s = MakeBlackbody(AsReal(in(0).pull()), (unsigned)d.params[0]); break;
     case LGPU_NODE_SURFACE_INFO: r.v[0] = ev.hit->normalS.x; r.v[1] = ev.hit->normalS.y; r.v[2] = ev.hit->normalS.z; break;
+    case LGPU_NODE_IMAGE_TEXTURE: {   /* ImageTextureInput::GetColour / GetScalar (GraphInputs.cpp:128-136) */
+        const int ti = (int)d.params[0];
+        const std::vector<float> &t = g.tex[ti];
+        const int w = g.texW[ti], h = g.texH[ti];
+        const V2 uv(Fract(ev.hit->uv.x), Fract(ev.hit->uv.y));
+        /* texture_t::GetPixelUVBilinear (Texture.h:71-81) */
+        const Real fx = std::min((float)(w - 1), clampr(uv.x, 0.f, 1.f) * (float)w);
+        const Real fy = std::min((float)(h - 1), clampr(uv.y, 0.f, 1.f) * (float)h);
+        const unsigned x = (unsigned)fx, y = (unsigned)fy;
+        const unsigned x1 = std::min(x + 1, (unsigned)w - 1), y1 = std::min(y + 1, (unsigned)h - 1);
+        for (int k = 0; k < 4; ++k) {
+            const Real ya = Lerp(t[4 * ((size_t)y * w + x) + k], t[4 * ((size_t)y * w + x1) + k], fx - (float)x);
+            const Real yb = Lerp(t[4 * ((size_t)y1 * w + x) + k], t[4 * ((size_t)y1 * w + x1) + k], fx - (float)x);
+            r.v[k] = Lerp(ya, yb, fy - (float)y);
+        }
+        if (out == 1) { r.v[1] = r.v[2] = r.v[3] = 0; }
+        break;
+    }
     case LGPU_NODE_SEPARATE_XYZ: {        /* B14: every output reads input 0 */
         const V3 v = AsVec3(in(0).pull());
         r.v[0] = out == 0 ? v.x : (out == 1 ? v.y : v.z);
@@ -2097,6 +2118,12 @@ static void Inverse3(const Real *m, Real *inv) {
 
 bool Oracle::Load(const lgpu_scene_desc *d) {
     sc.graph.nodes.assign(d->nodes, d->nodes + d->num_nodes);
+    for (int t = 0; t < d->num_textures; ++t) {
+        const lgpu_texture_desc &td = d->textures[t];
+        sc.graph.tex.emplace_back(td.rgba, td.rgba + (size_t)td.width * td.height * 4);
+        sc.graph.texW.push_back(td.width);
+        sc.graph.texH.push_back(td.height);
+    }
     sc.hasVolumes = d->has_volumes != 0;
     sc.meshes.resize(d->num_meshes);
     for (int i = 0; i < d->num_meshes; ++i) {

@@ -101,3 +101,16 @@ def test_wavefront_equals_megakernel_terrain(gpu_lib):
     frac, _ = path_agreement(a, b, rel=1e-5)
     assert frac >= 0.999
     np.testing.assert_array_equal(b, c)
+
+
+@MODES
+def test_inverse_cornell_texture_medium_paths(gpu_lib, mode):
+    """Image-textured back wall (bilinear at fract(uv)), GGX sphere and a medium cube."""
+    from lambda_gb300 import configs
+    sb, cams, opts = configs.cornell_inverse(40, 40, 4, tex_res=16)
+    opts.kernel_mode = mode
+    for cam in (cams[0], cams[4]):
+        g, o = _render_both(gpu_lib, sb, cam, opts, 40 * 40 * 4)
+        frac, _ = path_agreement(g, o)
+        assert np.isfinite(g).all()
+        assert frac >= 0.99, "per-path agreement %.5f" % frac

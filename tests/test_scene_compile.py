@@ -48,9 +48,24 @@ def test_bad_scene_rejected(lg):
 
 
 def test_unsupported_node_rejected(lg):
+    """MicrofacetBTDF has no reference implementation: rejected with a clear status."""
     sb, cam, opts = configs.cornell(8, 8, 1)
-    tex = sb.node("IMAGE_TEXTURE")
-    bx = sb.node("BXDF_LAMBERTIAN", inputs={0: lg.out(tex)})
+    bx = sb.node("BXDF_MICROFACET_T", [0, 1.5], {0: (0.9, 0.9, 0.9, 1), 1: 0.2})
     sb.materials[0] = (bx, -1, -1, -1)
     rc, rep = lg.scene_check(sb)
     assert rc != 0 and "unsupported" in rep
+
+
+def test_image_texture_needs_a_scene_texture(lg):
+    sb, cam, opts = configs.cornell(8, 8, 1)
+    tex = sb.node("IMAGE_TEXTURE", [3])       # no texture 3 in the scene
+    bx = sb.node("BXDF_LAMBERTIAN", inputs={0: lg.out(tex)})
+    sb.materials[0] = (bx, -1, -1, -1)
+    rc, rep = lg.scene_check(sb)
+    assert rc != 0 and "texture" in rep
+
+
+def test_image_texture_scene_compiles(lg):
+    sb, cams, opts = configs.cornell_inverse(16, 16, 1, tex_res=8)
+    rc, rep = lg.scene_check(sb)
+    assert rc == 0, rep
