@@ -393,6 +393,25 @@ typedef struct lgpu_tuning {
 LGPU_API int lgpu_autotune(lgpu_context *ctx, const lgpu_view_desc *views, int32_t n_views,
                            const lgpu_render_opts *opts, int32_t probe_spp, lgpu_tuning *out);
 
+/* Parameters the path-replay adjoint differentiates (any of them may be -1: not differentiated). */
+typedef struct lgpu_adjoint_desc {
+    int32_t tex_material;     /* material whose Lambertian albedo reads an IMAGE_TEXTURE ... */
+    int32_t texture;          /* ... of this scene texture: per-texel gradients */
+    int32_t rough_material;   /* material whose first BSDF leaf's roughness gets a gradient */
+    int32_t medium;           /* homogeneous medium whose (grey) sigma_a and sigma_s get gradients */
+} lgpu_adjoint_desc;
+
+/* Path-replay adjoint of one render (no counterpart in the reference, which has no derivatives).
+ * For the image I = lgpu_render_device(camera, opts) (pixel means over opts->spp samples) and a
+ * loss with dloss_dev = dLoss/dI (DEVICE, width * height float4, rgb used), ADDS dLoss/dtheta into
+ * grad_texture_dev (DEVICE, texture width * height float4, rgb) and grad_scalars_dev (DEVICE,
+ * 3 floats: roughness, sigma_a, sigma_s).  Every path is recomputed with the same random numbers
+ * as the forward render (nothing is stored between the passes); sampling decisions are treated
+ * as fixed.  RGB3 only; the forward render must use the same opts and seed.  Returns when done. */
+LGPU_API int lgpu_adjoint(lgpu_context *ctx, const lgpu_camera_desc *camera, const lgpu_render_opts *opts,
+                          const lgpu_adjoint_desc *params, const float *dloss_dev, float *grad_texture_dev,
+                          float *grad_scalars_dev, void *stream);
+
 /* Fixed-scratch variant of lgpu_render_paths, for callers that must not allocate.
  * No counterpart in the reference, which renders on the CPU.
  *

@@ -17,7 +17,7 @@ LIB_PATH = HERE / "_build" / "liblambda_gpu.so"
 
 EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_scene_commit", "lgpu_render",
            "lgpu_render_device", "lgpu_render_paths", "lgpu_render_count", "lgpu_intersect",
-           "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc", "lgpu_render_batch", "lgpu_autotune"]
+           "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc", "lgpu_render_batch", "lgpu_autotune", "lgpu_adjoint"]
 
 _lib = None
 
@@ -56,6 +56,8 @@ def lib():
         L.lgpu_version.restype = C.c_char_p
         L.lgpu_scene_check.argtypes = [C.POINTER(abi.SceneDesc), C.c_char_p, C.c_size_t]
         L.lgpu_render_batch.argtypes = [vp, C.POINTER(abi.ViewDesc), C.c_int32, C.POINTER(abi.RenderOpts), vp]
+        L.lgpu_adjoint.argtypes = [vp, C.POINTER(abi.CameraDesc), C.POINTER(abi.RenderOpts),
+                                   C.POINTER(abi.AdjointDesc), vp, vp, vp, vp]
         L.lgpu_autotune.argtypes = [vp, C.POINTER(abi.ViewDesc), C.c_int32, C.POINTER(abi.RenderOpts), C.c_int32,
                                     C.POINTER(abi.Tuning)]
         _lib = L
@@ -148,6 +150,15 @@ class Renderer:
         arr = self._views([v[:6] + (v[6] if len(v) > 6 else None,) for v in views])
         self._check(lib().lgpu_autotune(self._h, arr, len(views), C.byref(opts), probe_spp, C.byref(t)))
         return {f: getattr(t, f) for f, _ in abi.Tuning._fields_ if not f.startswith("pad")}
+
+    def adjoint(self, camera, opts, params, dloss_ptr, grad_tex_ptr, grad_scalars_ptr, stream=None):
+        """lgpu_adjoint: params = (tex_material, texture, rough_material, medium); pointers are device
+        addresses (ints); gradients are added into the given buffers."""
+        cam = camera.desc()
+        p = abi.AdjointDesc(*params)
+        self._check(lib().lgpu_adjoint(self._h, C.byref(cam), C.byref(opts), C.byref(p), C.c_void_p(dloss_ptr),
+                                       C.c_void_p(grad_tex_ptr) if grad_tex_ptr else None,
+                                       C.c_void_p(grad_scalars_ptr), C.c_void_p(stream) if stream else None))
 
     def render_count(self, camera, opts):
         cam = camera.desc()

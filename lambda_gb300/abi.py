@@ -90,6 +90,11 @@ class Tuning(C.Structure):
                 ("mpaths_per_s", C.c_double), ("tried", C.c_int32), ("pad2", C.c_int32)]
 
 
+class AdjointDesc(C.Structure):
+    _fields_ = [("tex_material", C.c_int32), ("texture", C.c_int32), ("rough_material", C.c_int32),
+                ("medium", C.c_int32)]
+
+
 class RenderOpts(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
                 ("max_bounces", C.c_int32), ("min_bounces", C.c_int32), ("integrator", C.c_int32),

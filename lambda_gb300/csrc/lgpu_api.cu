@@ -40,6 +40,8 @@ struct lgpu_context {
     DeviceScene S;
     bool have_scene = false;
     lgpu_stats stats;
+    std::vector<int> tex_off, tex_w, tex_h;   /* image textures of the committed scene */
+    int num_media = 0, num_materials = 0;
     bool tuned = false;         /* lgpu_autotune result, used by kernel_mode AUTO */
     lgpu_tuning tuning;
     unsigned long long *d_counters = nullptr;
@@ -121,6 +123,7 @@ inline lt::V3f v3(const float *p) { lt::V3f r; r.x = p[0]; r.y = p[1]; r.z = p[2
  * validate_scene checks every index a kernel will follow, lgpu_scene_commit uploads it. */
 struct HostScene {
     DeviceScene S;
+    std::vector<int> texOff, texW, texH;   /* image textures in the texel pool */
     std::vector<DNode> nodes;
     std::vector<DTri> tris;
     std::vector<DInst> insts;
@@ -550,11 +553,13 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
     /* ---------------- materials */
     std::vector<DIns> &code = H.code;
     /* image textures first: their texels share the float4 pool of the environment map */
-    std::vector<int> texOff;
+    std::vector<int> &texOff = H.texOff;
     for (int t = 0; t < d->num_textures; ++t) {
         const lgpu_texture_desc &td = d->textures[t];
         if (!td.rgba || td.width <= 0 || td.height <= 0) return fail(c, LGPU_ERR_INVALID_SCENE, "image texture without texels");
         texOff.push_back((int)H.envTex.size());
+        H.texW.push_back(td.width);
+        H.texH.push_back(td.height);
         for (int k = 0; k < td.width * td.height; ++k)
             H.envTex.push_back(make_float4(td.rgba[4 * k], td.rgba[4 * k + 1], td.rgba[4 * k + 2], td.rgba[4 * k + 3]));
     }
@@ -821,6 +826,9 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
               upload(c, envTex, &S.env_tex, bytes) && upload(c, media, &S.media, bytes);
     if (!ok) { free_scene(c); return c->err.find("alloc") != std::string::npos ? LGPU_ERR_OOM : LGPU_ERR_CUDA; }
     c->S = S;
+    c->tex_off = H.texOff; c->tex_w = H.texW; c->tex_h = H.texH;
+    c->num_media = (int)H.media.size();
+    c->num_materials = (int)H.mats.size();
     c->have_scene = true;
     c->stats.bvh_nodes = nodes.size();
     c->stats.bvh_bytes = nodes.size() * sizeof(DNode);
@@ -1520,6 +1528,51 @@ LGPU_API int lgpu_autotune(lgpu_context *c, const lgpu_view_desc *views, int32_t
     c->tuned = true;
     *out = c->tuning;
     return LGPU_OK;
+}
+
+}  // extern "C"
+
+/* ------------------------------------------------------------------ path-replay adjoint */
+extern "C" {
+
+LGPU_API int lgpu_adjoint(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o,
+                          const lgpu_adjoint_desc *p, const float *dloss_dev, float *grad_texture_dev,
+                          float *grad_scalars_dev, void *stream) {
+    int r = check_opts(c, cam, o);
+    if (r) return r;
+    if (!p || !dloss_dev || !grad_scalars_dev) return fail(c, LGPU_ERR_INVALID_ARG, "null adjoint buffers");
+    if (o->spectral_mode != LGPU_SPECTRAL_RGB3) return fail(c, LGPU_ERR_INVALID_ARG, "the adjoint is implemented for RGB3 only");
+    AdjArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.dloss = reinterpret_cast<const float4 *>(dloss_dev);
+    A.grad_tex = reinterpret_cast<float4 *>(grad_texture_dev);
+    A.grad_scalar = grad_scalars_dev;
+    A.tex_material = -1; A.rough_material = -1; A.medium = -1;
+    if (p->tex_material >= 0) {
+        if (p->tex_material >= c->num_materials || p->texture < 0 || p->texture >= (int)c->tex_off.size())
+            return fail(c, LGPU_ERR_INVALID_ARG, "adjoint texture or material out of range");
+        if (!grad_texture_dev) return fail(c, LGPU_ERR_INVALID_ARG, "null texture gradient");
+        A.tex_material = p->tex_material;
+        A.tex_off = c->tex_off[p->texture]; A.tex_w = c->tex_w[p->texture]; A.tex_h = c->tex_h[p->texture];
+    }
+    if (p->rough_material >= c->num_materials) return fail(c, LGPU_ERR_INVALID_ARG, "adjoint roughness material out of range");
+    if (p->medium >= c->num_media) return fail(c, LGPU_ERR_INVALID_ARG, "adjoint medium out of range");
+    A.rough_material = p->rough_material;
+    A.medium = p->medium;
+    A.inv_spp = 1.f / (float)o->spp;
+    cudaSetDevice(c->device);
+    RenderParams rp;
+    rp.spp = o->spp; rp.max_bounces = o->max_bounces; rp.min_bounces = o->min_bounces;
+    rp.seed = o->seed; rp.sample_offset = o->sample_offset;
+    const uint64_t n = (uint64_t)o->width * o->height * o->spp;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEventRecord(c->ev0, st);
+    cudaError_t e = launch_adjoint(c->S, make_cam(cam, o), rp, A, n, st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "adjoint launch");
+    cudaEventRecord(c->ev1, st);
+    c->stats.paths = n;
+    c->stats.launches = 1;
+    return finish_timing(c);
 }
 
 }  // extern "C"

@@ -17,12 +17,24 @@ struct LRef { int light, tri; };
 #define LG_MAX_TREE_DEPTH 64
 HD bool lref_eq(LRef a, LRef b) { return a.light == b.light && a.tri == b.tri; }
 
+/* Adjoint replay arguments: dLoss/dI per pixel and the gradient targets. */
+struct AdjArgs {
+    const float4 *dloss;   /* per pixel: dLoss / d(pixel mean), rgb */
+    float4 *grad_tex;      /* per texel of the differentiated texture (rgb accumulated) */
+    float *grad_scalar;    /* roughness, sigma_a, sigma_s (accumulated) */
+    int tex_material, tex_off, tex_w, tex_h;
+    int rough_material, medium;
+    float inv_spp;
+};
+
 template <int NS, bool COUNT>
 struct Tracer {
     const DeviceScene &S;
     Rng &rng;
     const Lambda4 &lam;
     TravStats *st;
+    float *trlen = nullptr;   /* adjoint replay: accumulates the path length inside medium trmed */
+    int trmed = -1;
 
     /* ---------------------------------------------------------------- scene queries */
     __device__ bool intersect(float3 o, float3 d, RayHit &h) {   /* Scene::Intersect (Scene.cpp:28-43) */
@@ -51,6 +63,7 @@ struct Tracer {
                 if (term) { const float delta = tFar - maxT; tFar -= delta; h.tFar -= delta; }
             }
             if (med >= 0 && Tr) *Tr *= medium_tr<NS>(S.media[med], h.tFar);
+            if (trlen && med >= 0 && med == trmed) *trlen += h.tFar;
             const DMaterial &m = mat(h);
             if (term || m.has_bsdf || m.light >= 0) { h.tFar = tFar; return true; }
             med = get_medium(m, d, h.nG);
@@ -503,6 +516,257 @@ struct Tracer {
             }
         }
         return Ld;
+    }
+
+    /* ---------------------------------------------------------------- path-replay adjoint
+     * The same estimator as Li, replayed with the same random numbers, carrying forward the
+     * log-derivatives of the path throughput with respect to the differentiated parameters:
+     * every radiance contribution C added to L credits dLoss/dI . C . dlnC/dtheta to the
+     * gradient.  Sampling decisions are held fixed (detached): the derivative of an estimator
+     * f L / p with p fixed is (df / f) f L / p, and MIS weights summing to one need no derivative.
+     * Parameters: texels of an image-texture albedo (Lambertian, linear), the roughness of one
+     * material's first BSDF leaf (central difference of the BSDF value), the grey sigma_a and
+     * sigma_s of one homogeneous medium (transmittance exp(-sigma_t len) and the sigma_s factor of
+     * a scattering event).  RGB3 only. */
+    struct TexEntry { int idx[4]; float w[4]; float3 inv; };
+
+    __device__ void credit(const AdjArgs &A, const TexEntry *E, int ne, const Spec<NS> &C, float3 dl,
+                           const Spec<NS> &Dr, const Spec<NS> &Dsa, const Spec<NS> &Dss, float g[3]) {
+        const float cx = dl.x * C.c[0], cy = dl.y * C.c[1], cz = dl.z * C.c[2];
+        g[0] += cx * Dr.c[0] + cy * Dr.c[1] + cz * Dr.c[2];
+        g[1] += cx * Dsa.c[0] + cy * Dsa.c[1] + cz * Dsa.c[2];
+        g[2] += cx * Dss.c[0] + cy * Dss.c[1] + cz * Dss.c[2];
+        for (int e = 0; e < ne; ++e) {
+            const float gx = cx * E[e].inv.x, gy = cy * E[e].inv.y, gz = cz * E[e].inv.z;
+            for (int t = 0; t < 4; ++t) {
+                if (E[e].w[t] == 0.f) continue;
+                float *q = reinterpret_cast<float *>(&A.grad_tex[E[e].idx[t]]);
+                atomicAdd(q + 0, gx * E[e].w[t]);
+                atomicAdd(q + 1, gy * E[e].w[t]);
+                atomicAdd(q + 2, gz * E[e].w[t]);
+            }
+        }
+    }
+    /* d ln f / d roughness of leaf 0 at the event's (woL, wiL): central difference */
+    __device__ Spec<NS> dlnf_rough(const Bsdf<NS> &b, const Event &ev) {
+        const float r = b.rough[0], h = 1e-3f * fmaxf(r, 0.05f);
+        Bsdf<NS> bp = b, bm = b;
+        bp.rough[0] = r + h;
+        bm.rough[0] = r - h;
+        const Spec<NS> f0 = bsdf_f<NS>(b, ev), fp = bsdf_f<NS>(bp, ev), fm = bsdf_f<NS>(bm, ev);
+        Spec<NS> d(0.f);
+        for (int c = 0; c < NS; ++c) d.c[c] = f0.c[c] > 0.f ? (fp.c[c] - fm.c[c]) / (2.f * h * f0.c[c]) : 0.f;
+        return d;
+    }
+    /* LdMediumPoint split into its light-sampled and phase-sampled terms, with the length each
+     * term's transmittance spent inside the differentiated medium */
+    __device__ void ld_medium_point_adj(Event &ev, RayHit &hit, float3 p, LRef lsLight, float3 lsPoint, float3 lsNormal,
+                                        Spec<NS> lsLe, float &lsPdf, float3 &wiOut, float3 sp, float3 sn,
+                                        Spec<NS> &T1, float &len1, Spec<NS> &T2, float &len2) {
+        const DMedium &med = S.media[ev.medium];
+        float partialLightPDF = lsPdf;
+        hit.point = p;
+        *trlen = 0.f;
+        Spec<NS> Li = lsLe * visibility(lsLight, p, ev, hit, lsPoint, lsNormal, lsPdf);
+        len1 = *trlen;
+        float scatteringPDF, lightPDF = lsPdf;
+        T1 = Spec<NS>(0.f);
+        T2 = Spec<NS>(0.f);
+        if (lightPDF > 0.f && !Li.black()) {
+            scatteringPDF = phase_hg(dot(ev.wo, ev.wi), med.g);
+            if (scatteringPDF > 0.f) {
+                const float w = power_heuristic(lightPDF, scatteringPDF);
+                T1 += Li * Spec<NS>(scatteringPDF) * w / lightPDF;
+            }
+        }
+        scatteringPDF = hg_sample(med.g, ev.wo, &ev.wi, rng);
+        wiOut = ev.wi;
+        const float3 ro = p, rd = ev.wi;
+        Spec<NS> Tr(1.f);
+        *trlen = 0.f;
+        const bool hs = intersect_tr(ro, rd, hit, ev.medium, &Tr, -1.f);
+        len2 = *trlen;
+        if (scatteringPDF > 0.f) {
+            LRef nl; nl.light = hs ? mat(hit).light : S.env_light; nl.tri = -1;
+            if (nl.light >= 0) {
+                if (!lref_eq(nl, lsLight)) partialLightPDF = light_pdf(sp, sn, hit.prim, nl);
+                lightPDF = partialLightPDF * pdf_li(nl, ev, hit);
+                Li = hs ? light_L(nl, ev, hit) : light_Le(nl, rd);
+                const float w = power_heuristic(scatteringPDF, lightPDF);
+                if (!Li.black() && lightPDF > 0.f) T2 += Li * Tr * w / scatteringPDF;
+            }
+        }
+    }
+
+    /* Replay of Li (same control flow and random numbers) accumulating gradients; g = (roughness,
+     * sigma_a, sigma_s), texel gradients go to A.grad_tex with atomics.  dl = dLoss/dI of the
+     * path's pixel divided by the samples per pixel.  Returns the replayed radiance. */
+    __device__ Spec<NS> Li_adj(float3 ro, float3 rd, int maxBounces, int minBounces, const AdjArgs &A, float3 dl, float g[3]) {
+        Spec<NS> L(0.f), beta(1.f);
+        Spec<NS> Dr(0.f), Dsa(0.f), Dss(0.f);   /* log-derivatives of beta */
+        const Spec<NS> zero(0.f);
+        TexEntry E[8];
+        int ne = 0;
+        float seglen = 0.f;
+        trlen = &seglen;
+        trmed = A.medium;
+        const float invSigS = (A.medium >= 0 && S.media[A.medium].ss[0] > 0.f) ? 1.f / S.media[A.medium].ss[0] : 0.f;
+        RayHit hit;
+        hit.tFar = finf(); hit.uv = make_float2(0.f, 0.f);
+        Event ev;
+        ev.wo = -rd; ev.wi = mk(0.f, 0.f, 0.f); ev.woL = ev.wi; ev.wiL = ev.wi;
+        ev.sidedness = 1; ev.medium = -1; ev.eta = 1.001f; ev.mediumInteraction = false;
+        bool scatterIntersect = false;
+        int nullCrossings = 0;
+        for (int bounces = 0; bounces < maxBounces; ++bounces) {
+            if (bounces == 0 ? intersect(ro, rd, hit) : scatterIntersect) {
+                if (bounces == 0) {
+                    const int li = mat(hit).light;
+                    if (li >= 0) {
+                        LRef lr; lr.light = li; lr.tri = -1;
+                        if (ev.medium >= 0) {
+                            const Spec<NS> C = light_L(lr, ev, hit) * medium_tr<NS>(S.media[ev.medium], hit.tFar);
+                            L += C;
+                            if (ev.medium == A.medium) credit(A, E, 0, C, dl, zero, Spec<NS>(-hit.tFar), Spec<NS>(-hit.tFar), g);
+                        } else L += light_L(lr, ev, hit);
+                    }
+                }
+                if (ev.medium >= 0) {
+                    const DMedium &med = S.media[ev.medium];
+                    const bool dm = ev.medium == A.medium;
+                    float lsPdf = 1.f;
+                    const float3 sp = hit.point, sn = hit.nS;
+                    const LRef lsLight = sample_light(hit.point, hit.nS, &lsPdf);
+                    float3 lsPoint, lsNormal = mk(0.f, 0.f, 0.f);
+                    const Spec<NS> lsLe = sample_point(lsLight, ev, hit, lsPoint, lsNormal, lsPdf);
+                    const int choice = (rng.next() > 0.5f) ? 0 : 1;
+                    float distT, distPdf, eqT, eqPdf;
+                    const Spec<NS> mTrD = medium_sample_distance<NS>(med, rng, ev, hit, &distT, &distPdf);
+                    const bool intD = ev.mediumInteraction;
+                    const Spec<NS> mTrE = medium_sample_equiangular<NS>(med, ro, rd, rng, ev, hit, lsPoint, &eqT, &eqPdf);
+                    const bool intE = ev.mediumInteraction;
+                    ev.mediumInteraction = intD && intE;
+                    if (!ev.mediumInteraction) {
+                        beta *= mTrD;
+                        if (dm) { Dsa += Spec<NS>(-distT); Dss += Spec<NS>(-distT); }
+                    }
+                    if (ev.mediumInteraction) {
+                        ev.wo = -rd;
+                        const float3 mpD = ro + rd * distT, mpE = ro + rd * eqT;
+                        const float distPdf2 = medium_pdf_distance<NS>(med, eqT);
+                        const float eqPdf2 = medium_pdf_equiangular(ro, rd, lsPoint, hit.tFar, distT);
+                        const float distW = power_heuristic(distPdf, eqPdf2);
+                        const float eqW = power_heuristic(eqPdf, distPdf2);
+                        float3 wiD, wiE;
+                        Spec<NS> t1, t2;
+                        float l1, l2;
+                        /* the reference adds the medium-vertex estimate to L without the throughput */
+                        ld_medium_point_adj(ev, hit, mpD, lsLight, lsPoint, lsNormal, lsLe, lsPdf, wiD, sp, sn, t1, l1, t2, l2);
+                        const float sD = dm ? -distT : 0.f, sE = dm ? -eqT : 0.f, ks = dm ? invSigS : 0.f;
+                        Spec<NS> C = t1 * mTrD * distW;
+                        L += C;
+                        credit(A, E, 0, C, dl, zero, Spec<NS>(sD - l1), Spec<NS>(sD - l1 + ks), g);
+                        C = t2 * mTrD * distW;
+                        L += C;
+                        credit(A, E, 0, C, dl, zero, Spec<NS>(sD - l2), Spec<NS>(sD - l2 + ks), g);
+                        ld_medium_point_adj(ev, hit, mpE, lsLight, lsPoint, lsNormal, lsLe, lsPdf, wiE, sp, sn, t1, l1, t2, l2);
+                        C = t1 * mTrE * eqW;
+                        L += C;
+                        credit(A, E, 0, C, dl, zero, Spec<NS>(sE - l1), Spec<NS>(sE - l1 + ks), g);
+                        C = t2 * mTrE * eqW;
+                        L += C;
+                        credit(A, E, 0, C, dl, zero, Spec<NS>(sE - l2), Spec<NS>(sE - l2 + ks), g);
+                        ro = choice == 0 ? mpD : mpE;
+                        rd = choice == 0 ? wiD : wiE;
+                        scatterIntersect = intersect(ro, rd, hit);
+                        beta *= (choice == 0 ? mTrD : mTrE);
+                        const float s = choice == 0 ? sD : sE;
+                        Dsa += Spec<NS>(s);
+                        Dss += Spec<NS>(s + ks);
+                    }
+                } else ev.mediumInteraction = false;
+
+                if (!ev.mediumInteraction) {
+                    const DMaterial &m = mat(hit);
+                    const int mi = S.objects[hit.obj].material;
+                    if (m.has_bsdf) {
+                        ev.wo = -rd;
+                        ev.woL = ev_local(hit, ev.wo);
+                        ev.wiL = ev_local(hit, ev.wi);
+                        ev.sidedness = (ev.woL.y > 0.f) ? 1 : -1;
+                        Bsdf<NS> b;
+                        setup_bsdf(b, m, ev, hit);
+                        if (mi == A.tex_material && ne < 8) {   /* albedo = bilinear texel blend */
+                            TexEntry &e = E[ne++];
+                            image_bilinear(S.env_tex, A.tex_off, A.tex_w, A.tex_h, hit.uv, e.idx, e.w);
+                            const Spec<NS> a = b.alb[0];
+                            e.inv = make_float3(a.c[0] > 0.f ? 1.f / a.c[0] : 0.f, a.c[1] > 0.f ? 1.f / a.c[1] : 0.f,
+                                                a.c[2] > 0.f ? 1.f / a.c[2] : 0.f);
+                        }
+                        const bool dr = mi == A.rough_material;
+                        float lightDistPdf = 1.f;
+                        const float3 sp = hit.point, sn = hit.nS;
+                        const LRef l = sample_light(hit.point, hit.nS, &lightDistPdf);
+                        Spec<NS> LdN(0.f), LdS(0.f), DrN(0.f), DrS(0.f);
+                        float scatteringPDF = 0.f, lightPDF = 0.f;
+                        seglen = 0.f;
+                        Spec<NS> Li = sample_li(l, ev, hit, lightPDF);
+                        const float lenN = seglen;
+                        Spec<NS> f;
+                        lightPDF *= lightDistPdf;
+                        if (lightPDF > 0.f && !Li.black()) {
+                            f = bsdf_f<NS>(b, ev) * fabsf(ev.wiL.y);
+                            scatteringPDF = bsdf_pdf<NS>(b, ev.woL, ev.wiL);
+                            if (!f.black() && scatteringPDF > 0.f) {
+                                const float w = power_heuristic(lightPDF, scatteringPDF);
+                                LdN += Li * f * w / lightPDF;
+                                if (dr) DrN = dlnf_rough(b, ev);
+                            }
+                        }
+                        f = bsdf_sample<NS>(b, ev, hit, rng, scatteringPDF);
+                        f *= fabsf(ev.wiL.y);
+                        if (dr) DrS = dlnf_rough(b, ev);
+                        ro = hit.point;
+                        rd = ev.wi;
+                        ev.medium = get_medium(m, ev.wi, hit.nG);
+                        scatterIntersect = intersect(ro, rd, hit);
+                        if (scatteringPDF > 0.f && !f.black()) {
+                            LRef nl; nl.light = scatterIntersect ? mat(hit).light : S.env_light; nl.tri = -1;
+                            if (nl.light >= 0) {
+                                if (!lref_eq(nl, l)) lightDistPdf = light_pdf(sp, sn, hit.prim, nl);
+                                lightPDF = lightDistPdf * pdf_li(nl, ev, hit);
+                                Li = scatterIntersect ? light_L(nl, ev, hit) : light_Le(nl, rd);
+                                const float w = power_heuristic(scatteringPDF, lightPDF);
+                                if (!Li.black() && lightPDF > 0.f) LdS += Li * f * w / scatteringPDF;
+                            }
+                        } else break;
+                        const Spec<NS> CN = beta * LdN, CS = beta * LdS;
+                        L += CN + CS;
+                        credit(A, E, ne, CN, dl, Dr + DrN, Dsa + Spec<NS>(-lenN), Dss + Spec<NS>(-lenN), g);
+                        credit(A, E, ne, CS, dl, Dr + DrS, Dsa, Dss, g);
+                        beta *= f / scatteringPDF;
+                        Dr += DrS;
+                    } else {
+                        ev.medium = get_medium(m, rd, hit.nG);
+                        ro = hit.point + hit.nG * (dot(hit.nG, rd) < 0.f ? -SURFACE_EPSILON : SURFACE_EPSILON);
+                        if (bounces > 0) scatterIntersect = intersect(ro, rd, hit);
+                        if (++nullCrossings > 256) break;
+                        bounces--;
+                        continue;
+                    }
+                }
+                if (bounces > minBounces) {
+                    const float q = smax(.05f, 1.f - spec_y<NS>(beta, lam));
+                    if (rng.next() < q) break;
+                    beta /= 1.f - q;
+                }
+            } else {
+                if (bounces == 0 && S.env_light >= 0) L += env_le(rd) * beta;
+                break;
+            }
+        }
+        trlen = nullptr;
+        return L;
     }
 
     /* MISVolumetricPathIntegrator::Li (MISVolumetricPathIntegrator.cpp:71-215) */

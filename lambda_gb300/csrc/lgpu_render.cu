@@ -118,6 +118,46 @@ __global__ void __launch_bounds__(128) k_render(const __grid_constant__ DeviceSc
 }
 
 #if LGPU_NS == 3 && LGPU_COUNT == 0
+/* Path-replay adjoint: one thread per path of the frame, the forward path recomputed with the same
+ * random numbers while gradients of the image loss are accumulated (Tracer::Li_adj). */
+__global__ void __launch_bounds__(128) k_adjoint(const __grid_constant__ DeviceScene S, const __grid_constant__ CamParams cam,
+                                                 const __grid_constant__ RenderParams rp, const __grid_constant__ AdjArgs A,
+                                                 uint64_t n) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float g[3] = {0.f, 0.f, 0.f};
+    if (i < n) {
+        const uint32_t pixel = (uint32_t)(i / (uint64_t)rp.spp);
+        const uint32_t sidx = (uint32_t)(i % (uint64_t)rp.spp) + rp.sample_offset;
+        const uint32_t x = pixel % (uint32_t)cam.W, y = pixel / (uint32_t)cam.W;
+        Rng rng;
+        rng.key = lgpu_path_key(rp.seed, pixel, sidx);
+        rng.dim = 0;
+        Lambda4 lam;
+        const float u = cam.xi * ((float)x + rng.next() - .5f);
+        const float v = cam.yi * ((float)y + rng.next() - .5f);
+        const float3 p = cam.o + cam.x * (u * -cam.tanFov2 + cam.tanFov) +
+                         cam.y * (v * -cam.tanFov2 * cam.aspect + cam.tanFov * cam.aspect) + cam.z;
+        const float3 d = normalised(p - cam.o);
+        const float4 dd = A.dloss[pixel];
+        const float3 dl = make_float3(dd.x * A.inv_spp, dd.y * A.inv_spp, dd.z * A.inv_spp);
+        TravStats st = {0u, 0u, 0u};
+        Tracer<3, false> T{S, rng, lam, &st};
+        T.Li_adj(cam.o, d, rp.max_bounces, rp.min_bounces, A, dl, g);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float s = g[k];
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if ((threadIdx.x & 31) == 0 && s != 0.f) atomicAdd(&A.grad_scalar[k], s);
+    }
+}
+cudaError_t launch_adjoint(const DeviceScene &S, const CamParams &cam, const RenderParams &rp, const AdjArgs &A,
+                           uint64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_adjoint<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S, cam, rp, A, n);
+    return cudaGetLastError();
+}
+
 /* Closest-hit queries for a ray batch (Scene::Intersect restated; tnear = 0, tfar = inf). */
 __global__ void k_intersect(const __grid_constant__ DeviceScene S, const float4 *rays, uint4 *hits, float2 *uvs, uint64_t n) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -54,6 +54,9 @@ def test_ctypes_layout_matches_header(tmp_path):
                "lgpu_render_opts": abi.RenderOpts, "lgpu_stats": abi.Stats}
     if hasattr(abi, "ViewDesc"):
         structs["lgpu_view_desc"] = abi.ViewDesc
+    if hasattr(abi, "AdjointDesc"):
+        structs["lgpu_adjoint_desc"] = abi.AdjointDesc
+        structs["lgpu_texture_desc"] = abi.TextureDesc
     if hasattr(abi, "Tuning"):
         structs["lgpu_tuning"] = abi.Tuning
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "lambda_gpu.h"', "int main(void) {"]
