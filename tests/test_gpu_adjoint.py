@@ -1,0 +1,101 @@
+"""Path-replay adjoint (lgpu_adjoint) against common-random-number central finite differences of the
+forward render, on the inverse-rendering Cornell box (textured back wall, GGX sphere, medium cube).
+
+Loss: L = sum over pixels of w . I with fixed random weights w, so dL/dI = w.  The finite
+difference re-renders with the same seed at theta +- eps (eps = 1e-3).  The adjoint holds sampling
+decisions fixed while the finite difference moves them, so the two agree only up to Monte Carlo
+noise: both are taken at 64x64 pixels x 128 spp and compared within 5 % relative."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+W = H = 64
+SPP = 128
+EPS = 1e-3
+TOL = 0.05
+CAM = 3
+
+
+def _setup(torch, lg, configs, **kw):
+    sb, cams, opts = configs.cornell_inverse(W, H, SPP, tex_res=8, **kw)
+    opts.kernel_mode = 1          # megakernel: the estimator the adjoint replays
+    r = lg.Renderer(sb)
+    return r, cams[CAM], opts
+
+
+def _loss(torch, lg, configs, w, **kw):
+    r, cam, opts = _setup(torch, lg, configs, **kw)
+    try:
+        film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        r.render_device(cam, opts, film.data_ptr())
+        torch.cuda.synchronize()
+        f = film.double().cpu().numpy()
+        img = f[..., :3] / f[..., 3:4]
+        return float(np.sum(img * w))
+    finally:
+        r.close()
+
+
+def _adjoint(torch, lg, configs, w, **kw):
+    r, cam, opts = _setup(torch, lg, configs, **kw)
+    try:
+        dloss = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        dloss[..., :3] = torch.from_numpy(w.astype(np.float32)).cuda()
+        gtex = torch.zeros((8, 8, 4), dtype=torch.float32, device="cuda")
+        gsc = torch.zeros(3, dtype=torch.float32, device="cuda")
+        # material indices of cornell_inverse: 0 = textured back wall, 4 = GGX sphere; medium 0
+        r.adjoint(cam, opts, (0, 0, 4, 0), dloss.data_ptr(), gtex.data_ptr(), gsc.data_ptr())
+        torch.cuda.synchronize()
+        return gtex.cpu().numpy()[..., :3].astype(np.float64), gsc.cpu().numpy().astype(np.float64)
+    finally:
+        r.close()
+
+
+@pytest.fixture(scope="module")
+def setup(gpu_lib):
+    torch = pytest.importorskip("torch")
+    from lambda_gb300 import configs
+    rng = np.random.RandomState(11)
+    w = rng.uniform(0.0, 1.0, (H, W, 3))
+    albedo = rng.uniform(0.1, 0.9, (8, 8, 3)).astype(np.float32)
+    base = dict(albedo=albedo, roughness=0.3, sigma_a=0.1, sigma_s=0.8)
+    gtex, gsc = _adjoint(torch, gpu_lib, configs, w, **base)
+    return torch, configs, w, base, gtex, gsc
+
+
+def _fd(setup, lg, **delta):
+    torch, configs, w, base, _, _ = setup
+    plus, minus = dict(base), dict(base)
+    for k, v in delta.items():
+        plus[k] = base[k] + EPS * v
+        minus[k] = base[k] - EPS * v
+    return (_loss(torch, lg, configs, w, **plus) - _loss(torch, lg, configs, w, **minus)) / (2 * EPS)
+
+
+def test_adjoint_texture_direction(setup, gpu_lib):
+    _, _, _, base, gtex, _ = setup
+    v = np.random.RandomState(3).uniform(-1, 1, (8, 8, 3)).astype(np.float32)
+    fd = _fd(setup, gpu_lib, albedo=v)
+    adj = float(np.sum(gtex * v))
+    assert np.isfinite(adj) and abs(adj - fd) <= TOL * abs(fd), (adj, fd)
+
+
+@pytest.mark.parametrize("name,idx", [("roughness", 0), ("sigma_a", 1), ("sigma_s", 2)])
+def test_adjoint_scalars(setup, gpu_lib, name, idx):
+    _, _, _, base, _, gsc = setup
+    fd = _fd(setup, gpu_lib, **{name: 1.0})
+    assert np.isfinite(gsc[idx]) and abs(gsc[idx] - fd) <= TOL * abs(fd) + 1e-6, (name, gsc[idx], fd)
+
+
+def test_adjoint_rejects_hero_mode(gpu_lib):
+    torch = pytest.importorskip("torch")
+    from lambda_gb300 import abi, configs
+    r, cam, opts = _setup(torch, gpu_lib, configs)
+    try:
+        opts.spectral_mode = abi.SPECTRAL_HERO4
+        buf = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        with pytest.raises(gpu_lib.LambdaGPUError, match="RGB3"):
+            r.adjoint(cam, opts, (0, 0, 4, 0), buf.data_ptr(), buf.data_ptr(), buf.data_ptr())
+    finally:
+        r.close()
