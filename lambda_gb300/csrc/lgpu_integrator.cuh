@@ -647,8 +647,10 @@ struct Tracer {
                     const bool intE = ev.mediumInteraction;
                     ev.mediumInteraction = intD && intE;
                     if (!ev.mediumInteraction) {
+                        /* the distance sample's weight: Tr / P(pass) past the segment, or, when only
+                         * the equiangular sample left the segment, the scattering form Tr sigma_s / pdf */
                         beta *= mTrD;
-                        if (dm) { Dsa += Spec<NS>(-distT); Dss += Spec<NS>(-distT); }
+                        if (dm) { Dsa += Spec<NS>(-distT); Dss += Spec<NS>(-distT + (intD ? invSigS : 0.f)); }
                     }
                     if (ev.mediumInteraction) {
                         ev.wo = -rd;

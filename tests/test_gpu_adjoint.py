@@ -4,28 +4,32 @@ forward render, on the inverse-rendering Cornell box (textured back wall, GGX sp
 Loss: L = sum over pixels of w . I with fixed random weights w, so dL/dI = w.  The finite
 difference re-renders with the same seed at theta +- eps (eps = 1e-3).  The adjoint holds sampling
 decisions fixed while the finite difference moves them, so the two agree only up to Monte Carlo
-noise: both are taken at 64x64 pixels x 128 spp and compared within 5 % relative."""
+noise: both are taken at 64x64 pixels x 512 spp and compared within 5 % relative.  The forward
+renders for the differences use the wavefront (deterministic per-pixel summation order)."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 W = H = 64
-SPP = 128
+SPP = 512
 EPS = 1e-3
 TOL = 0.05
 CAM = 3
 
 
-def _setup(torch, lg, configs, **kw):
+def _setup(torch, lg, configs, no_rr=False, **kw):
     sb, cams, opts = configs.cornell_inverse(W, H, SPP, tex_res=8, **kw)
     opts.kernel_mode = 1          # megakernel: the estimator the adjoint replays
+    if no_rr:
+        opts.min_bounces = opts.max_bounces   # no Russian roulette: albedo moves no sampling decision
     r = lg.Renderer(sb)
     return r, cams[CAM], opts
 
 
-def _loss(torch, lg, configs, w, **kw):
-    r, cam, opts = _setup(torch, lg, configs, **kw)
+def _loss(torch, lg, configs, w, no_rr=False, **kw):
+    r, cam, opts = _setup(torch, lg, configs, no_rr, **kw)
+    opts.kernel_mode = 2          # same paths as the megakernel, film summed in a fixed order
     try:
         film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
         r.render_device(cam, opts, film.data_ptr())
@@ -37,8 +41,8 @@ def _loss(torch, lg, configs, w, **kw):
         r.close()
 
 
-def _adjoint(torch, lg, configs, w, **kw):
-    r, cam, opts = _setup(torch, lg, configs, **kw)
+def _adjoint(torch, lg, configs, w, no_rr=False, **kw):
+    r, cam, opts = _setup(torch, lg, configs, no_rr, **kw)
     try:
         dloss = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
         dloss[..., :3] = torch.from_numpy(w.astype(np.float32)).cuda()
@@ -61,20 +65,31 @@ def setup(gpu_lib):
     albedo = rng.uniform(0.1, 0.9, (8, 8, 3)).astype(np.float32)
     base = dict(albedo=albedo, roughness=0.3, sigma_a=0.1, sigma_s=0.8)
     gtex, gsc = _adjoint(torch, gpu_lib, configs, w, **base)
-    return torch, configs, w, base, gtex, gsc
+    gtex_nr, _ = _adjoint(torch, gpu_lib, configs, w, no_rr=True, **base)
+    return torch, configs, w, base, gtex, gsc, gtex_nr
 
 
-def _fd(setup, lg, **delta):
-    torch, configs, w, base, _, _ = setup
+def _fd(setup, lg, no_rr=False, **delta):
+    torch, configs, w, base = setup[:4]
     plus, minus = dict(base), dict(base)
     for k, v in delta.items():
         plus[k] = base[k] + EPS * v
         minus[k] = base[k] - EPS * v
-    return (_loss(torch, lg, configs, w, **plus) - _loss(torch, lg, configs, w, **minus)) / (2 * EPS)
+    return (_loss(torch, lg, configs, w, no_rr, **plus) - _loss(torch, lg, configs, w, no_rr, **minus)) / (2 * EPS)
+
+
+def test_adjoint_texture_direction_exact(setup, gpu_lib):
+    """Without Russian roulette the albedo moves no sampling decision: the common-random-number
+    difference is the same estimator's derivative, so adjoint and difference agree to 1e-3."""
+    gtex_nr = setup[6]
+    v = np.random.RandomState(3).uniform(-1, 1, (8, 8, 3)).astype(np.float32)
+    fd = _fd(setup, gpu_lib, no_rr=True, albedo=v)
+    adj = float(np.sum(gtex_nr * v))
+    assert np.isfinite(adj) and abs(adj - fd) <= 1e-3 * abs(fd) + 1e-6, (adj, fd)
 
 
 def test_adjoint_texture_direction(setup, gpu_lib):
-    _, _, _, base, gtex, _ = setup
+    gtex = setup[4]
     v = np.random.RandomState(3).uniform(-1, 1, (8, 8, 3)).astype(np.float32)
     fd = _fd(setup, gpu_lib, albedo=v)
     adj = float(np.sum(gtex * v))
@@ -83,7 +98,7 @@ def test_adjoint_texture_direction(setup, gpu_lib):
 
 @pytest.mark.parametrize("name,idx", [("roughness", 0), ("sigma_a", 1), ("sigma_s", 2)])
 def test_adjoint_scalars(setup, gpu_lib, name, idx):
-    _, _, _, base, _, gsc = setup
+    gsc = setup[5]
     fd = _fd(setup, gpu_lib, **{name: 1.0})
     assert np.isfinite(gsc[idx]) and abs(gsc[idx] - fd) <= TOL * abs(fd) + 1e-6, (name, gsc[idx], fd)
 
