@@ -329,7 +329,6 @@ def main_inverse(args):
     def scene(params, seed):
         sb, cams, opts = configs.cornell_inverse(Wd, Ht, spp, **params)
         opts.seed = seed
-        opts.kernel_mode = 1
         return lg.Renderer(sb), cams, opts
 
     films = [torch.zeros((Ht, Wd, 4), dtype=torch.float32, device="cuda") for _ in range(8)]
@@ -347,7 +346,7 @@ def main_inverse(args):
     gsc = torch.zeros(3, dtype=torch.float32, device="cuda")
     dloss = [torch.zeros((Ht, Wd, 4), dtype=torch.float32, device="cuda") for _ in range(8)]
     fwd_t, bwd_t, losses = [], [], []
-    steps = max(3, args.steps)
+    steps = max(8, args.steps)
     for it in range(args.warmup + steps):
         r, cams, opts = scene(cur, 1 + it)
         torch.cuda.synchronize()
@@ -376,9 +375,10 @@ def main_inverse(args):
         losses.append(loss)
         g = gtex.cpu().numpy()[..., :3]
         s_ = gsc.cpu().numpy()
-        cur["albedo"] = np.clip(cur["albedo"] - 2e3 * g, 0.02, 0.98).astype(np.float32)
-        cur["roughness"] = float(np.clip(cur["roughness"] - 2.0 * s_[0], 0.05, 1.0))
-        cur["sigma_s"] = float(np.clip(cur["sigma_s"] - 2.0 * s_[2], 0.01, 4.0))
+        # normalised gradient steps (each parameter group scaled by its gradient's rms)
+        cur["albedo"] = np.clip(cur["albedo"] - 0.05 * g / (np.sqrt(np.mean(g * g)) + 1e-30), 0.02, 0.98).astype(np.float32)
+        cur["roughness"] = float(np.clip(cur["roughness"] - 0.05 * np.sign(s_[0]), 0.05, 1.0))
+        cur["sigma_s"] = float(np.clip(cur["sigma_s"] - 0.1 * np.sign(s_[2]), 0.01, 4.0))
     paths = 8 * Wd * Ht * spp
     fwd, bwd = float(np.median(fwd_t)), float(np.median(bwd_t))
     line = {"metric": METRIC, "value": paths / fwd / 1e6, "unit": UNIT, "n_gpus": 1, "steps": steps,
