@@ -55,16 +55,17 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--width", type=int, default=1920)
-    p.add_argument("--height", type=int, default=1080)
-    p.add_argument("--spp", type=int, default=64)
+    p.add_argument("--width", type=int, default=0, help="0 = the workload's own size")
+    p.add_argument("--height", type=int, default=0)
+    p.add_argument("--spp", type=int, default=0)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--mode", default="auto", choices=["auto", "megakernel", "wavefront", "graph"])
     p.add_argument("--pool", type=int, default=0, help="wavefront path-slot pool size (0 = default)")
     p.add_argument("--block", type=int, default=0, help="trace-kernel block size (0 = default)")
-    p.add_argument("--workload", default="terrain", choices=["terrain", "batched", "inverse"],
-                   help="terrain: the 1080p many-light frame; batched: 64 uneven views of the terrain and "
+    p.add_argument("--workload", default="terrain", choices=["terrain", "volume", "cornell", "batched", "inverse"],
+                   help="terrain: the 1080p many-light frame (default); volume, cornell: the other two single-frame "
+                        "scenes; batched: 64 uneven views of the terrain and "
                         "volume scenes in one batched render against the same views one at a time")
     return p.parse_args()
 
@@ -230,6 +231,34 @@ def batched_views(seed=6, n=64):
             cam = Camera(o, (0.0, 2.0, 0.0), fov=0.9)
         out.append((scene, cam, res, res, spp, depth, 100 + i))
     return out
+
+
+# single-frame workloads: builder, default width, height, spp, depth and the config record
+SINGLE = {
+    "terrain": (lambda w, h, s: configs_mod().terrain(w, h, s, 6), 1920, 1080, 64, WORKLOAD),
+    "volume": (lambda w, h, s: configs_mod().volume(w, h, s, 12), 1280, 720, 128,
+               dict(workload="volumetric + instancing: homogeneous medium box (sigma_a 0.05, sigma_s 0.5, g 0.3), "
+                             "16 point + 4 spot lights, 1000 instances of a 100k-triangle displaced sphere, "
+                             "half dielectric, half Oren-Nayar/GGX mix", max_depth=12, triangles=100352,
+                    instances=1000, spectral="RGB3", light_sampler="light tree")),
+    "cornell": (lambda w, h, s: configs_mod().cornell(w, h, s, 8), 256, 256, 16,
+                dict(workload="Cornell box: 5 walls, icosphere (1280 tris, GGX 0.2), 6500 K quad light", max_depth=8,
+                     triangles=1292, spectral="RGB3", light_sampler="light tree")),
+}
+
+
+def configs_mod():
+    from lambda_gb300 import configs
+    return configs
+
+
+def workload_scene(args):
+    build, w0, h0, s0, rec = SINGLE[args.workload]
+    w, h, spp = args.width or w0, args.height or h0, args.spp or s0
+    sb, cam, opts = build(w, h, spp)
+    cfg = dict(rec)
+    cfg["width"], cfg["height"], cfg["spp"] = w, h, spp
+    return sb, cam, opts, cfg
 
 
 def main_batched(args):
@@ -407,7 +436,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        sb, cam, opts = configs.terrain(args.width, args.height, args.spp, 6)
+        sb, cam, opts, cfg = workload_scene(args)
         K, W_ = args.steps, args.warmup
         vals = []
         for i in range(W_ + K):
@@ -416,7 +445,6 @@ def main():
                 vals.append(cb["value"])
         v = float(np.median(vals))
         cb["value"] = v
-        cfg = dict(WORKLOAD)
         cfg["l2"] = "n/a (CPU)"
         print(json.dumps({"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": K, "warmup": W_,
                           "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -435,7 +463,7 @@ def main():
         dist.init_process_group("nccl")
     dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
-    sb, cam, opts = configs.terrain(args.width, args.height, args.spp, 6)
+    sb, cam, opts, cfg = workload_scene(args)
     opts.seed = replica_seed(rank)
     opts.kernel_mode = {"auto": abi.KERNEL_AUTO, "megakernel": abi.KERNEL_MEGAKERNEL, "wavefront": abi.KERNEL_WAVEFRONT,
                         "graph": abi.KERNEL_WAVEFRONT_GRAPH}[args.mode]
@@ -516,7 +544,6 @@ def main():
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(sb, cam, opts, args.cpu_seconds)
-    cfg = dict(WORKLOAD)
     cfg["l2"] = "scene data > L2 and a 256 MiB buffer is written between timed steps"
     cfg["width"], cfg["height"], cfg["spp"] = W, H, spp
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
