@@ -524,6 +524,9 @@ struct Tracer {
      * every radiance contribution C added to L credits dLoss/dI . C . dlnC/dtheta to the
      * gradient.  Sampling decisions are held fixed (detached): the derivative of an estimator
      * f L / p with p fixed is (df / f) f L / p, and MIS weights summing to one need no derivative.
+     * The reference's MIS weights do not always sum to one over the strategies (its light pdf for
+     * a BSDF-sampled hit is the mesh light's, the sampled one the triangle's), so the weights are
+     * differentiated too: d ln w of the power heuristic through the parameter-dependent pdf.
      * Parameters: texels of an image-texture albedo (Lambertian, linear), the roughness of one
      * material's first BSDF leaf (central difference of the BSDF value), the grey sigma_a and
      * sigma_s of one homogeneous medium (transmittance exp(-sigma_t len) and the sigma_s factor of
@@ -557,6 +560,14 @@ struct Tracer {
         Spec<NS> d(0.f);
         for (int c = 0; c < NS; ++c) d.c[c] = f0.c[c] > 0.f ? (fp.c[c] - fm.c[c]) / (2.f * h * f0.c[c]) : 0.f;
         return d;
+    }
+    /* d pdf / d roughness of leaf 0 at the event's directions: central difference */
+    __device__ float dpdf_rough(const Bsdf<NS> &b, const Event &ev) {
+        const float r = b.rough[0], h = 1e-3f * fmaxf(r, 0.05f);
+        Bsdf<NS> bp = b, bm = b;
+        bp.rough[0] = r + h;
+        bm.rough[0] = r - h;
+        return (bsdf_pdf<NS>(bp, ev.woL, ev.wiL) - bsdf_pdf<NS>(bm, ev.woL, ev.wiL)) / (2.f * h);
     }
     /* LdMediumPoint split into its light-sampled and phase-sampled terms, with the length each
      * term's transmittance spent inside the differentiated medium */
@@ -665,19 +676,28 @@ struct Tracer {
                         /* the reference adds the medium-vertex estimate to L without the throughput */
                         ld_medium_point_adj(ev, hit, mpD, lsLight, lsPoint, lsNormal, lsLe, lsPdf, wiD, sp, sn, t1, l1, t2, l2);
                         const float sD = dm ? -distT : 0.f, sE = dm ? -eqT : 0.f, ks = dm ? invSigS : 0.f;
+                        /* MIS weights through the distance-sampling pdf sigma_t exp(-sigma_t t) */
+                        float wD = 0.f, wE = 0.f;
+                        if (dm) {
+                            const float sigT = S.media[A.medium].sa[0] + S.media[A.medium].ss[0];
+                            const float a2 = distPdf * distPdf, b2 = eqPdf2 * eqPdf2;
+                            const float c2 = eqPdf * eqPdf, d2 = distPdf2 * distPdf2;
+                            if (a2 + b2 > 0.f) wD = 2.f * (1.f / sigT - distT) * b2 / (a2 + b2);
+                            if (c2 + d2 > 0.f) wE = -2.f * (1.f / sigT - eqT) * d2 / (c2 + d2);
+                        }
                         Spec<NS> C = t1 * mTrD * distW;
                         L += C;
-                        credit(A, E, 0, C, dl, zero, Spec<NS>(sD - l1), Spec<NS>(sD - l1 + ks), g);
+                        credit(A, E, 0, C, dl, zero, Spec<NS>(sD - l1 + wD), Spec<NS>(sD - l1 + ks + wD), g);
                         C = t2 * mTrD * distW;
                         L += C;
-                        credit(A, E, 0, C, dl, zero, Spec<NS>(sD - l2), Spec<NS>(sD - l2 + ks), g);
+                        credit(A, E, 0, C, dl, zero, Spec<NS>(sD - l2 + wD), Spec<NS>(sD - l2 + ks + wD), g);
                         ld_medium_point_adj(ev, hit, mpE, lsLight, lsPoint, lsNormal, lsLe, lsPdf, wiE, sp, sn, t1, l1, t2, l2);
                         C = t1 * mTrE * eqW;
                         L += C;
-                        credit(A, E, 0, C, dl, zero, Spec<NS>(sE - l1), Spec<NS>(sE - l1 + ks), g);
+                        credit(A, E, 0, C, dl, zero, Spec<NS>(sE - l1 + wE), Spec<NS>(sE - l1 + ks + wE), g);
                         C = t2 * mTrE * eqW;
                         L += C;
-                        credit(A, E, 0, C, dl, zero, Spec<NS>(sE - l2), Spec<NS>(sE - l2 + ks), g);
+                        credit(A, E, 0, C, dl, zero, Spec<NS>(sE - l2 + wE), Spec<NS>(sE - l2 + ks + wE), g);
                         ro = choice == 0 ? mpD : mpE;
                         rd = choice == 0 ? wiD : wiE;
                         scatterIntersect = intersect(ro, rd, hit);
@@ -722,12 +742,17 @@ struct Tracer {
                             if (!f.black() && scatteringPDF > 0.f) {
                                 const float w = power_heuristic(lightPDF, scatteringPDF);
                                 LdN += Li * f * w / lightPDF;
-                                if (dr) DrN = dlnf_rough(b, ev);
+                                if (dr) {
+                                    const float pL2 = lightPDF * lightPDF, pS = scatteringPDF;
+                                    DrN = dlnf_rough(b, ev) + Spec<NS>(-2.f * pS * dpdf_rough(b, ev) / (pL2 + pS * pS));
+                                }
                             }
                         }
                         f = bsdf_sample<NS>(b, ev, hit, rng, scatteringPDF);
                         f *= fabsf(ev.wiL.y);
-                        if (dr) DrS = dlnf_rough(b, ev);
+                        float dpS = 0.f;
+                        if (dr) { DrS = dlnf_rough(b, ev); dpS = dpdf_rough(b, ev); }
+                        Spec<NS> DwS(0.f);
                         ro = hit.point;
                         rd = ev.wi;
                         ev.medium = get_medium(m, ev.wi, hit.nG);
@@ -739,13 +764,19 @@ struct Tracer {
                                 lightPDF = lightDistPdf * pdf_li(nl, ev, hit);
                                 Li = scatterIntersect ? light_L(nl, ev, hit) : light_Le(nl, rd);
                                 const float w = power_heuristic(scatteringPDF, lightPDF);
-                                if (!Li.black() && lightPDF > 0.f) LdS += Li * f * w / scatteringPDF;
+                                if (!Li.black() && lightPDF > 0.f) {
+                                    LdS += Li * f * w / scatteringPDF;
+                                    if (dr) {
+                                        const float pL2 = lightPDF * lightPDF, pS = scatteringPDF;
+                                        DwS = Spec<NS>(2.f * dpS / pS * pL2 / (pL2 + pS * pS));
+                                    }
+                                }
                             }
                         } else break;
                         const Spec<NS> CN = beta * LdN, CS = beta * LdS;
                         L += CN + CS;
                         credit(A, E, ne, CN, dl, Dr + DrN, Dsa + Spec<NS>(-lenN), Dss + Spec<NS>(-lenN), g);
-                        credit(A, E, ne, CS, dl, Dr + DrS, Dsa, Dss, g);
+                        credit(A, E, ne, CS, dl, Dr + DrS + DwS, Dsa, Dss, g);
                         beta *= f / scatteringPDF;
                         Dr += DrS;
                     } else {
