@@ -865,8 +865,9 @@ int check_opts(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_o
     if (o->width <= 0 || o->height <= 0 || o->spp <= 0) return fail(c, LGPU_ERR_INVALID_ARG, "width, height and spp must be positive");
     if (o->max_bounces < 0 || o->min_bounces < 0) return fail(c, LGPU_ERR_INVALID_ARG, "negative bounce count");
     if ((uint64_t)o->width * o->height > (1ull << 32) - 1) return fail(c, LGPU_ERR_INVALID_ARG, "film too large");
-    if (o->integrator != LGPU_INTEGRATOR_GPU_MISVOLPATH && o->integrator != LGPU_INTEGRATOR_VOLPATH)
-        return fail(c, LGPU_ERR_INVALID_ARG, "integrator not available on the GPU path");
+    if (o->integrator < LGPU_INTEGRATOR_PATH || o->integrator > LGPU_INTEGRATOR_GPU_MISVOLPATH ||
+        o->integrator == LGPU_INTEGRATOR_AOV)
+        return fail(c, LGPU_ERR_INVALID_ARG, "integrator not available on the GPU path (AOV passes are not built)");
     return LGPU_OK;
 }
 
@@ -1113,7 +1114,11 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     return LGPU_OK;
 }
 
-bool use_wavefront(const lgpu_render_opts *o) { return o->kernel_mode != LGPU_KERNEL_MEGAKERNEL; }
+/* The wavefront state machine is the MIS volumetric integrator; the other integrators run as the
+ * megakernel. */
+bool use_wavefront(const lgpu_render_opts *o) {
+    return o->kernel_mode != LGPU_KERNEL_MEGAKERNEL && o->integrator == LGPU_INTEGRATOR_GPU_MISVOLPATH;
+}
 
 int ensure_paths(lgpu_context *c, size_t n) {
     if (c->w_paths_cap >= n) return LGPU_OK;
@@ -1193,6 +1198,7 @@ int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_
     a.rp.min_bounces = o->min_bounces;
     a.rp.seed = o->seed;
     a.rp.sample_offset = o->sample_offset;
+    a.rp.integrator = o->integrator;
     a.film = film;
     a.paths_out = paths;
     a.ids = ids;
@@ -1396,8 +1402,9 @@ LGPU_API int lgpu_render_batch(lgpu_context *c, const lgpu_view_desc *views, int
     const lgpu_render_opts eff = effective_opts(c, o_in);
     const lgpu_render_opts *o = &eff;
     if (!c->have_scene) return fail(c, LGPU_ERR_NO_SCENE, "no committed scene");
-    if (o->integrator != LGPU_INTEGRATOR_GPU_MISVOLPATH && o->integrator != LGPU_INTEGRATOR_VOLPATH)
-        return fail(c, LGPU_ERR_INVALID_ARG, "integrator not available on the GPU path");
+    if (o->integrator < LGPU_INTEGRATOR_PATH || o->integrator > LGPU_INTEGRATOR_GPU_MISVOLPATH ||
+        o->integrator == LGPU_INTEGRATOR_AOV)
+        return fail(c, LGPU_ERR_INVALID_ARG, "integrator not available on the GPU path (AOV passes are not built)");
     if (o->min_bounces < 0) return fail(c, LGPU_ERR_INVALID_ARG, "negative bounce count");
     for (int v = 0; v < n_views; ++v) {
         int r = check_view(c, views[v]);
@@ -1411,8 +1418,8 @@ LGPU_API int lgpu_render_batch(lgpu_context *c, const lgpu_view_desc *views, int
     c->stats.traced = c->stats.spawned = c->stats.launches = 0;
     cudaEventRecord(c->ev0, st);
     uint64_t all = 0;
-    if (o->kernel_mode == LGPU_KERNEL_MEGAKERNEL) {
-        /* one megakernel launch per view (the unbatched scheme) */
+    if (o->kernel_mode == LGPU_KERNEL_MEGAKERNEL || o->integrator != LGPU_INTEGRATOR_GPU_MISVOLPATH) {
+        /* one megakernel launch per view (the unbatched scheme; the only one for the non-MIS integrators) */
         for (int v = 0; v < n_views; ++v) {
             const lgpu_render_opts vo = view_opts(o, views[v]);
             const uint64_t n = (uint64_t)vo.width * vo.height * vo.spp;
@@ -1420,7 +1427,7 @@ LGPU_API int lgpu_render_batch(lgpu_context *c, const lgpu_view_desc *views, int
             a.S = c->S;
             a.cam = make_cam(&views[v].camera, &vo);
             a.rp.spp = vo.spp; a.rp.max_bounces = vo.max_bounces; a.rp.min_bounces = vo.min_bounces;
-            a.rp.seed = vo.seed; a.rp.sample_offset = vo.sample_offset;
+            a.rp.seed = vo.seed; a.rp.sample_offset = vo.sample_offset; a.rp.integrator = vo.integrator;
             a.film = reinterpret_cast<float4 *>(views[v].film_dev);
             a.paths_out = nullptr; a.ids = nullptr; a.n = n; a.counters = c->d_counters;
             a.hero = vo.spectral_mode == LGPU_SPECTRAL_HERO4;

@@ -518,6 +518,269 @@ struct Tracer {
         return Ld;
     }
 
+    /* ---------------------------------------------------------------- the other integrators
+     * PathIntegrator::Li (src/integrators/PathIntegrator.cpp:15-88): the surface branch of the MIS
+     * integrator with media ignored (null surfaces are crossed, no medium is entered).  B7 patched
+     * as in Li: the light-tree pdf of a BSDF-sampled emitter is evaluated at the shading point. */
+    __device__ Spec<NS> Li_path(float3 ro, float3 rd, int maxBounces, int minBounces) {
+        Spec<NS> L(0.f), beta(1.f);
+        RayHit hit;
+        hit.tFar = finf(); hit.uv = make_float2(0.f, 0.f);
+        Event ev;
+        ev.wo = -rd; ev.wi = mk(0.f, 0.f, 0.f); ev.woL = ev.wi; ev.wiL = ev.wi;
+        ev.sidedness = 1; ev.medium = -1; ev.eta = 1.001f; ev.mediumInteraction = false;
+        bool scatterIntersect = false;
+        int nullCrossings = 0;
+        for (int bounces = 0; bounces < maxBounces; ++bounces) {
+            if (bounces == 0 ? intersect(ro, rd, hit) : scatterIntersect) {
+                const DMaterial &m = mat(hit);
+                if (bounces == 0 && m.light >= 0) { LRef lr; lr.light = m.light; lr.tri = -1; L += light_L(lr, ev, hit); }
+                if (m.has_bsdf) {
+                    ev.wo = -rd;
+                    ev.woL = ev_local(hit, ev.wo);
+                    ev.wiL = ev_local(hit, ev.wi);
+                    ev.sidedness = (ev.woL.y > 0.f) ? 1 : -1;
+                    Bsdf<NS> b;
+                    setup_bsdf(b, m, ev, hit);
+                    float lightDistPdf = 1.f;
+                    const float3 sp = hit.point, sn = hit.nS;
+                    const LRef l = sample_light(hit.point, hit.nS, &lightDistPdf);
+                    Spec<NS> Ld(0.f);
+                    float scatteringPDF = 0.f, lightPDF = 0.f;
+                    Spec<NS> Li = sample_li(l, ev, hit, lightPDF);
+                    Spec<NS> f;
+                    lightPDF *= lightDistPdf;
+                    if (lightPDF > 0.f && !Li.black()) {
+                        f = bsdf_f<NS>(b, ev) * fabsf(ev.wiL.y);
+                        scatteringPDF = bsdf_pdf<NS>(b, ev.woL, ev.wiL);
+                        if (!f.black() && scatteringPDF > 0.f) Ld += Li * f * power_heuristic(lightPDF, scatteringPDF) / lightPDF;
+                    }
+                    f = bsdf_sample<NS>(b, ev, hit, rng, scatteringPDF);
+                    f *= fabsf(ev.wiL.y);
+                    ro = hit.point;
+                    rd = ev.wi;
+                    scatterIntersect = intersect(ro, rd, hit);
+                    if (scatteringPDF > 0.f && !f.black()) {
+                        LRef nl; nl.light = scatterIntersect ? mat(hit).light : S.env_light; nl.tri = -1;
+                        if (nl.light >= 0) {
+                            if (!lref_eq(nl, l)) lightDistPdf = light_pdf(sp, sn, hit.prim, nl);
+                            lightPDF = lightDistPdf * pdf_li(nl, ev, hit);
+                            Li = scatterIntersect ? light_L(nl, ev, hit) : light_Le(nl, rd);
+                            if (!Li.black() && lightPDF > 0.f) Ld += Li * f * power_heuristic(scatteringPDF, lightPDF) / scatteringPDF;
+                        }
+                    } else break;
+                    L += beta * Ld;
+                    beta *= f / scatteringPDF;
+                } else {
+                    ro = hit.point + hit.nG * (dot(rd, hit.nG) < 0.f ? -SURFACE_EPSILON : SURFACE_EPSILON);
+                    if (bounces > 0) scatterIntersect = intersect(ro, rd, hit);
+                    if (++nullCrossings > 256) break;
+                    bounces--;
+                    continue;
+                }
+                if (bounces > minBounces) {
+                    const float q = smax(.05f, 1.f - spec_y<NS>(beta, lam));
+                    if (rng.next() < q) break;
+                    beta /= 1.f - q;
+                }
+            } else {
+                if (bounces == 0 && S.env_light >= 0) L += env_le(rd);
+                break;
+            }
+        }
+        return L;
+    }
+
+    /* VolumetricPathIntegrator::Li (src/integrators/VolumetricPathIntegrator.cpp:20-160): distance
+     * sampling only (no equiangular), medium vertices with light sampling + phase MIS, the medium
+     * contribution weighted by the throughput.  B7 patched at surface and medium vertices; an
+     * absent environment light contributes nothing on escape (the reference dereferences null). */
+    __device__ Spec<NS> Li_volpath(float3 ro, float3 rd, int maxBounces, int minBounces) {
+        Spec<NS> L(0.f), beta(1.f);
+        RayHit hit;
+        hit.tFar = finf(); hit.uv = make_float2(0.f, 0.f);
+        Event ev;
+        ev.wo = -rd; ev.wi = mk(0.f, 0.f, 0.f); ev.woL = ev.wi; ev.wiL = ev.wi;
+        ev.sidedness = 1; ev.medium = -1; ev.eta = 1.001f; ev.mediumInteraction = false;
+        bool scatterIntersect = false;
+        int nullCrossings = 0;
+        for (int bounces = 0; bounces < maxBounces; ++bounces) {
+            if (bounces == 0 ? intersect(ro, rd, hit) : scatterIntersect) {
+                if (bounces == 0 && mat(hit).light >= 0) {
+                    LRef lr; lr.light = mat(hit).light; lr.tri = -1;
+                    if (ev.medium >= 0) L += light_L(lr, ev, hit) * medium_tr<NS>(S.media[ev.medium], hit.tFar);
+                    else L += light_L(lr, ev, hit);
+                }
+                float distanceT = 0.f, distPdf = 0.f;
+                if (ev.medium >= 0) beta *= medium_sample_distance<NS>(S.media[ev.medium], rng, ev, hit, &distanceT, &distPdf);
+                else ev.mediumInteraction = false;
+                if (!ev.mediumInteraction) {
+                    const DMaterial &m = mat(hit);
+                    if (m.has_bsdf) {
+                        ev.wo = -rd;
+                        ev.woL = ev_local(hit, ev.wo);
+                        ev.wiL = ev_local(hit, ev.wi);
+                        ev.sidedness = (ev.woL.y > 0.f) ? 1 : -1;
+                        Bsdf<NS> b;
+                        setup_bsdf(b, m, ev, hit);
+                        float lightDistPdf = 1.f;
+                        const float3 sp = hit.point, sn = hit.nS;
+                        const LRef l = sample_light(hit.point, hit.nS, &lightDistPdf);
+                        Spec<NS> Ld(0.f);
+                        float scatteringPDF = 0.f, lightPDF = 0.f;
+                        Spec<NS> Li = sample_li(l, ev, hit, lightPDF);
+                        Spec<NS> f;
+                        lightPDF *= lightDistPdf;
+                        if (lightPDF > 0.f && !Li.black()) {
+                            f = bsdf_f<NS>(b, ev) * fabsf(ev.wiL.y);
+                            scatteringPDF = bsdf_pdf<NS>(b, ev.woL, ev.wiL);
+                            if (!f.black() && scatteringPDF > 0.f) Ld += Li * f * power_heuristic(lightPDF, scatteringPDF) / lightPDF;
+                        }
+                        f = bsdf_sample<NS>(b, ev, hit, rng, scatteringPDF);
+                        f *= fabsf(ev.wiL.y);
+                        ro = hit.point;
+                        rd = ev.wi;
+                        ev.medium = get_medium(m, ev.wi, hit.nG);
+                        scatterIntersect = intersect(ro, rd, hit);
+                        if (scatteringPDF > 0.f && !f.black()) {
+                            LRef nl; nl.light = scatterIntersect ? mat(hit).light : S.env_light; nl.tri = -1;
+                            if (nl.light >= 0) {
+                                if (!lref_eq(nl, l)) lightDistPdf = light_pdf(sp, sn, hit.prim, nl);
+                                lightPDF = lightDistPdf * pdf_li(nl, ev, hit);
+                                Li = scatterIntersect ? light_L(nl, ev, hit) : light_Le(nl, rd);
+                                if (!Li.black() && lightPDF > 0.f) Ld += Li * f * power_heuristic(scatteringPDF, lightPDF) / scatteringPDF;
+                            }
+                        } else break;
+                        L += beta * Ld;
+                        beta *= f / scatteringPDF;
+                    } else {
+                        ev.medium = get_medium(m, rd, hit.nG);
+                        ro = hit.point + hit.nG * (dot(hit.nG, rd) < 0.f ? -SURFACE_EPSILON : SURFACE_EPSILON);
+                        if (bounces > 0) scatterIntersect = intersect(ro, rd, hit);
+                        if (++nullCrossings > 256) break;
+                        bounces--;
+                        continue;
+                    }
+                } else if (ev.medium >= 0) {
+                    const DMedium &med = S.media[ev.medium];
+                    ev.wo = -rd;
+                    const float3 scatterPoint = ro + rd * distanceT;
+                    hit.point = scatterPoint;   /* the surface hit's normal stays (the reference reuses the hit) */
+                    float lightDistPdf = 1.f;
+                    const float3 sp = hit.point, sn = hit.nS;
+                    const LRef l = sample_light(hit.point, hit.nS, &lightDistPdf);
+                    Spec<NS> Ld(0.f);
+                    float scatteringPDF = 0.f, lightPDF = 0.f;
+                    Spec<NS> Li = sample_li(l, ev, hit, lightPDF);
+                    lightPDF *= lightDistPdf;
+                    if (lightPDF > 0.f && !Li.black()) {
+                        scatteringPDF = phase_hg(dot(ev.wo, ev.wi), med.g);
+                        if (scatteringPDF > 0.f) Ld += Li * Spec<NS>(scatteringPDF) * power_heuristic(lightPDF, scatteringPDF) / lightPDF;
+                    }
+                    scatteringPDF = hg_sample(med.g, ev.wo, &ev.wi, rng);
+                    ro = hit.point;
+                    rd = ev.wi;
+                    Spec<NS> Tr(1.f);
+                    scatterIntersect = intersect_tr(ro, rd, hit, ev.medium, &Tr, -1.f);
+                    if (scatteringPDF > 0.f) {
+                        LRef nl; nl.light = scatterIntersect ? mat(hit).light : S.env_light; nl.tri = -1;
+                        if (nl.light >= 0) {
+                            if (!lref_eq(nl, l)) lightDistPdf = light_pdf(sp, sn, hit.prim, nl);
+                            lightPDF = lightDistPdf * pdf_li(nl, ev, hit);
+                            Li = scatterIntersect ? light_L(nl, ev, hit) : light_Le(nl, rd);
+                            if (!Li.black() && lightPDF > 0.f) Ld += Li * Tr * power_heuristic(scatteringPDF, lightPDF) / scatteringPDF;
+                        }
+                    } else break;
+                    ro = scatterPoint;
+                    scatterIntersect = intersect(ro, rd, hit);
+                    L += beta * Ld;
+                }
+                if (bounces > minBounces) {
+                    const float q = smax(.05f, 1.f - spec_y<NS>(beta, lam));
+                    if (rng.next() < q) break;
+                    beta /= 1.f - q;
+                }
+            } else {
+                if (bounces == 0 && S.env_light >= 0) L += env_le(rd) * beta;
+                break;
+            }
+        }
+        return L;
+    }
+
+    /* DirectLightingIntegrator::Li (src/integrators/DirectLightingIntegrator.cpp:13-29) with
+     * Integrator::SampleOneLight / EstimateDirect (src/integrators/Integrator.cpp:5-55).  The
+     * reference's quirks are kept: the BSDF-sampled light pdf is PDF_Li at the shading point, and
+     * the BSDF-sampled hit counts only if its light is the sampled light object itself.  Null surfaces
+     * are crossed with a 1e-4 offset (at most 256 times); an absent environment light gives 0. */
+    __device__ Spec<NS> Li_direct(float3 ro, float3 rd) {
+        RayHit hit;
+        hit.tFar = finf(); hit.uv = make_float2(0.f, 0.f);
+        for (int guard = 0; guard < 256; ++guard) {
+            if (!intersect(ro, rd, hit)) return S.env_light >= 0 ? env_le(rd) : Spec<NS>(0.f);
+            const DMaterial &m = mat(hit);
+            if (!m.has_bsdf) { ro = hit.point + rd * .0001f; continue; }
+            Event ev;
+            ev.wo = -rd; ev.wi = mk(0.f, 0.f, 0.f);
+            ev.woL = ev_local(hit, ev.wo); ev.wiL = ev_local(hit, ev.wi);
+            ev.sidedness = (ev.woL.y > 0.f) ? 1 : -1; ev.medium = -1; ev.eta = 1.001f; ev.mediumInteraction = false;
+            Bsdf<NS> b;
+            setup_bsdf(b, m, ev, hit);
+            float lightPdf = 1.f;
+            const LRef l = sample_light(hit.point, hit.nS, &lightPdf);
+            if (l.light < 0) return Spec<NS>(0.f);
+            /* EstimateDirect */
+            Spec<NS> Ld(0.f);
+            float scatteringPDF = 0.f, lightPDF = 0.f;
+            Spec<NS> Li = sample_li(l, ev, hit, lightPDF);
+            if (lightPDF > 0.f && !Li.black()) {
+                const Spec<NS> f = bsdf_f<NS>(b, ev) * fabsf(ev.wiL.y);
+                scatteringPDF = bsdf_pdf<NS>(b, ev.woL, ev.wiL);
+                if (!f.black() && scatteringPDF > 0.f) Ld += Li * f * power_heuristic(lightPDF, scatteringPDF) / lightPDF;
+            }
+            Spec<NS> f = bsdf_sample<NS>(b, ev, hit, rng, scatteringPDF);   /* moves hit.point off the surface */
+            f *= fabsf(ev.wiL.y);
+            if (scatteringPDF > 0.f && !f.black()) {
+                lightPDF = pdf_li(l, ev, hit);
+                if (lightPDF == 0.f) return Ld / lightPdf;
+                const float w = power_heuristic(scatteringPDF, lightPDF);
+                const float3 o2 = hit.point + hit.nG * .00001f;
+                RayHit lh;
+                lh.tFar = finf(); lh.uv = make_float2(0.f, 0.f);
+                Spec<NS> Lc(0.f);
+                if (intersect(o2, ev.wi, lh)) {
+                    if (l.tri < 0 && mat(lh).light == l.light) {
+                        Event be = ev;
+                        be.wo = -ev.wi;
+                        LRef lr; lr.light = l.light; lr.tri = -1;
+                        Lc = light_L(lr, be, lh);
+                    }
+                } else {
+                    Lc = light_Le(l, ev.wi);
+                }
+                if (!Lc.black()) Ld += f * Lc * w / scatteringPDF;
+            }
+            return Ld / lightPdf;
+        }
+        return Spec<NS>(0.f);
+    }
+
+    /* UtilityIntegrator::Li of NormalPass (shading normal; the reference's green channel is
+     * n.y / 2 + 1) and DepthPass(max depth 100, power 1, background (1, 0, 1))
+     * (src/integrators/UtilityIntegrators.cpp:7-53), converted as Spectrum::FromRGB (reflectance). */
+    __device__ Spec<NS> Li_pass(float3 ro, float3 rd, bool normal) {
+        RayHit hit;
+        hit.tFar = finf(); hit.uv = make_float2(0.f, 0.f);
+        float3 c;
+        if (intersect(ro, rd, hit)) {
+            if (normal) c = mk(hit.nS.x * .5f + .5f, hit.nS.y * .5f + 1.f, hit.nS.z * .5f + .5f);
+            else { const float d = powf(mag(hit.point - ro) / 100.f, 1.f); c = mk(d, d, d); }
+        } else {
+            c = normal ? mk(0.f, 0.f, 0.f) : mk(1.f, 0.f, 1.f);
+        }
+        return from_rgb<NS>(c.x, c.y, c.z, false, lam);
+    }
+
     /* ---------------------------------------------------------------- path-replay adjoint
      * The same estimator as Li, replayed with the same random numbers, carrying forward the
      * log-derivatives of the path throughput with respect to the differentiated parameters:

@@ -15,6 +15,7 @@ struct CamParams {
 struct RenderParams {
     int spp, max_bounces, min_bounces;
     uint32_t seed, sample_offset;
+    int integrator;   /* lgpu_integrator (megakernel only; the wavefront runs the MIS integrator) */
 };
 /* One view of a batched render: its camera and parameters, and the index of its first path within
  * the chunk of views being rendered (paths of a view are pixel-major, spp per pixel). */

@@ -75,7 +75,15 @@ __global__ void __launch_bounds__(128) k_render(const __grid_constant__ DeviceSc
                          cam.y * (v * -cam.tanFov2 * cam.aspect + cam.tanFov * cam.aspect) + cam.z;
         const float3 d = normalised(p - cam.o);
         Tracer<NS, COUNT> T{S, rng, lam, &st};
-        const Spec<NS> L = T.Li(cam.o, d, rp.max_bounces, rp.min_bounces);
+        Spec<NS> L;
+        switch (rp.integrator) {
+        case LGPU_INTEGRATOR_PATH: L = T.Li_path(cam.o, d, rp.max_bounces, rp.min_bounces); break;
+        case LGPU_INTEGRATOR_VOLPATH: L = T.Li_volpath(cam.o, d, rp.max_bounces, rp.min_bounces); break;
+        case LGPU_INTEGRATOR_DIRECT: L = T.Li_direct(cam.o, d); break;
+        case LGPU_INTEGRATOR_NORMAL: L = T.Li_pass(cam.o, d, true); break;
+        case LGPU_INTEGRATOR_DEPTH: L = T.Li_pass(cam.o, d, false); break;
+        default: L = T.Li(cam.o, d, rp.max_bounces, rp.min_bounces); break;
+        }
         hero_to_rgb<NS>(L, lam, rgb);
         /* w = random numbers drawn: a control-flow fingerprint of the path */
         if (paths_out) paths_out[i] = make_float4(rgb[0], rgb[1], rgb[2], (float)rng.dim);

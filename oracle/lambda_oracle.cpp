@@ -1974,6 +1974,245 @@ struct Integrator {
         return Ld;
     }
 
+    /* PathIntegrator::Li (PathIntegrator.cpp:15-88); B7 patched (tree pdf at the shading point);
+     * at most 256 null-surface crossings. */
+    Spec LiPath(Ray r, Sampler &s) const {
+        Spec L(0), beta(1);
+        RayHit hit;
+        ScatterEvent ev;
+        ev.hit = &hit;
+        ev.scene = &sc;
+        ev.wo = -r.d;
+        bool scatterIntersect = false;
+        int nullCrossings = 0;
+        for (int bounces = 0; bounces < maxBounces; ++bounces) {
+            if (bounces == 0 ? sc.Intersect(r, hit) : scatterIntersect) {
+                if (bounces == 0 && Mat(hit).light) L += Mat(hit).light->L(ev);
+                const Material &m = Mat(hit);
+                if (m.bxdf >= 0) {
+                    ev.wo = -r.d;
+                    ev.SurfaceLocalise();
+                    Real lightDistPdf = 1;
+                    const V3 sp = hit.point, sn = hit.normalS;
+                    const LightBase *l = sc.lightSampler->Sample(ev, s, &lightDistPdf);
+                    Spec Ld(0);
+                    Real scatteringPDF = 0, lightPDF = 0;
+                    Spec f, Li = l ? l->Sample_Li(ev, s, lightPDF) : Spec(0);
+                    lightPDF *= lightDistPdf;
+                    if (lightPDF > 0 && !Li.IsBlack()) {
+                        f = bx.f(m.bxdf, ev) * std::abs(ev.wiL.y);
+                        scatteringPDF = bx.Pdf(m.bxdf, ev.woL, ev.wiL, ev);
+                        if (!f.IsBlack() && scatteringPDF > 0) Ld += Li * f * PowerHeuristic(lightPDF, scatteringPDF) / lightPDF;
+                    }
+                    f = bx.Sample_f(m.bxdf, ev, s, scatteringPDF);
+                    f *= std::abs(ev.wiL.y);
+                    r.o = hit.point;
+                    r.d = ev.wi;
+                    scatterIntersect = sc.Intersect(r, hit);
+                    if (scatteringPDF > 0 && !f.IsBlack()) {
+                        const LightBase *nl = scatterIntersect ? Mat(hit).light : sc.envLight;
+                        if (nl) {
+                            if (nl != l) lightDistPdf = sc.lightSampler->Pdf(sp, sn, hit.primId, nl);
+                            lightPDF = lightDistPdf * nl->PDF_Li(ev);
+                            Li = scatterIntersect ? nl->L(ev) : nl->Le(r);
+                            if (!Li.IsBlack() && lightPDF > 0) Ld += Li * f * PowerHeuristic(scatteringPDF, lightPDF) / scatteringPDF;
+                        }
+                    } else break;
+                    L += beta * Ld;
+                    beta *= f / scatteringPDF;
+                } else {
+                    r.o = hit.point + hit.normalG * (Dot(r.d, hit.normalG) < 0 ? -SURFACE_EPSILON : SURFACE_EPSILON);
+                    if (bounces > 0) scatterIntersect = sc.Intersect(r, hit);
+                    if (++nullCrossings > 256) break;
+                    bounces--;
+                    continue;
+                }
+                if (bounces > minBounces) {
+                    const Real q = smax((Real).05, 1 - beta.y());
+                    if (s.Get1D() < q) break;
+                    beta /= (Real)1 - q;
+                }
+            } else {
+                if (bounces == 0 && sc.envLight) L += sc.envLight->Le(r);
+                break;
+            }
+        }
+        return L;
+    }
+
+    /* VolumetricPathIntegrator::Li (VolumetricPathIntegrator.cpp:20-160); B7 patched at surface
+     * and medium vertices; no environment light: nothing on escape (the reference dereferences
+     * null); at most 256 null-surface crossings. */
+    Spec LiVolPath(Ray r, Sampler &s) const {
+        Spec L(0), beta(1);
+        RayHit hit;
+        ScatterEvent ev;
+        ev.hit = &hit;
+        ev.scene = &sc;
+        ev.wo = -r.d;
+        bool scatterIntersect = false;
+        int nullCrossings = 0;
+        ev.medium = nullptr;
+        for (int bounces = 0; bounces < maxBounces; ++bounces) {
+            if (bounces == 0 ? sc.Intersect(r, hit) : scatterIntersect) {
+                if (bounces == 0 && Mat(hit).light) {
+                    if (ev.medium) L += Mat(hit).light->L(ev) * ev.medium->Tr(hit.tFar);
+                    else L += Mat(hit).light->L(ev);
+                }
+                Real distanceT = 0, distPdf = 0;
+                if (ev.medium) beta *= ev.medium->SampleDistance(s, ev, &distanceT, &distPdf);
+                else ev.mediumInteraction = false;
+                if (!ev.mediumInteraction) {
+                    const Material &m = Mat(hit);
+                    if (m.bxdf >= 0) {
+                        ev.wo = -r.d;
+                        ev.SurfaceLocalise();
+                        Real lightDistPdf = 1;
+                        const V3 sp = hit.point, sn = hit.normalS;
+                        const LightBase *l = sc.lightSampler->Sample(ev, s, &lightDistPdf);
+                        Spec Ld(0);
+                        Real scatteringPDF = 0, lightPDF = 0;
+                        Spec f, Li = l ? l->Sample_Li(ev, s, lightPDF) : Spec(0);
+                        lightPDF *= lightDistPdf;
+                        if (lightPDF > 0 && !Li.IsBlack()) {
+                            f = bx.f(m.bxdf, ev) * std::abs(ev.wiL.y);
+                            scatteringPDF = bx.Pdf(m.bxdf, ev.woL, ev.wiL, ev);
+                            if (!f.IsBlack() && scatteringPDF > 0) Ld += Li * f * PowerHeuristic(lightPDF, scatteringPDF) / lightPDF;
+                        }
+                        f = bx.Sample_f(m.bxdf, ev, s, scatteringPDF);
+                        f *= std::abs(ev.wiL.y);
+                        r.o = hit.point;
+                        r.d = ev.wi;
+                        ev.medium = sc.GetMedium(m, ev.wi, hit.normalG);
+                        scatterIntersect = sc.Intersect(r, hit);
+                        if (scatteringPDF > 0 && !f.IsBlack()) {
+                            const LightBase *nl = scatterIntersect ? Mat(hit).light : sc.envLight;
+                            if (nl) {
+                                if (nl != l) lightDistPdf = sc.lightSampler->Pdf(sp, sn, hit.primId, nl);
+                                lightPDF = lightDistPdf * nl->PDF_Li(ev);
+                                Li = scatterIntersect ? nl->L(ev) : nl->Le(r);
+                                if (!Li.IsBlack() && lightPDF > 0) Ld += Li * f * PowerHeuristic(scatteringPDF, lightPDF) / scatteringPDF;
+                            }
+                        } else break;
+                        L += beta * Ld;
+                        beta *= f / scatteringPDF;
+                    } else {
+                        ev.medium = sc.GetMedium(m, r.d, hit.normalG);
+                        r.o = hit.point + hit.normalG * (Dot(hit.normalG, r.d) < 0 ? -SURFACE_EPSILON : SURFACE_EPSILON);
+                        if (bounces > 0) scatterIntersect = sc.Intersect(r, hit);
+                        if (++nullCrossings > 256) break;
+                        bounces--;
+                        continue;
+                    }
+                } else if (ev.medium) {
+                    ev.wo = -r.d;
+                    const V3 scatterPoint = r.o + r.d * distanceT;
+                    hit.point = scatterPoint;
+                    Real lightDistPdf = 1;
+                    const V3 sp = hit.point, sn = hit.normalS;
+                    const LightBase *l = sc.lightSampler->Sample(ev, s, &lightDistPdf);
+                    Spec Ld(0);
+                    Real scatteringPDF = 0, lightPDF = 0;
+                    Spec Li = l ? l->Sample_Li(ev, s, lightPDF) : Spec(0);
+                    lightPDF *= lightDistPdf;
+                    if (lightPDF > 0 && !Li.IsBlack()) {
+                        scatteringPDF = ev.medium->p(ev.wo, ev.wi);
+                        if (scatteringPDF > 0) Ld += Li * Spec(scatteringPDF) * PowerHeuristic(lightPDF, scatteringPDF) / lightPDF;
+                    }
+                    scatteringPDF = ev.medium->Sample_p(ev.wo, &ev.wi, s);
+                    r.o = hit.point;
+                    r.d = ev.wi;
+                    Spec Tr(1);
+                    const Medium *med = ev.medium;
+                    scatterIntersect = sc.IntersectTr(r, hit, s, med, &Tr);
+                    if (scatteringPDF > 0) {
+                        const LightBase *nl = scatterIntersect ? Mat(hit).light : sc.envLight;
+                        if (nl) {
+                            if (nl != l) lightDistPdf = sc.lightSampler->Pdf(sp, sn, hit.primId, nl);
+                            lightPDF = lightDistPdf * nl->PDF_Li(ev);
+                            Li = scatterIntersect ? nl->L(ev) : nl->Le(r);
+                            if (!Li.IsBlack() && lightPDF > 0) Ld += Li * Tr * PowerHeuristic(scatteringPDF, lightPDF) / scatteringPDF;
+                        }
+                    } else break;
+                    r.o = scatterPoint;
+                    scatterIntersect = sc.Intersect(r, hit);
+                    L += beta * Ld;
+                }
+                if (bounces > minBounces) {
+                    const Real q = smax((Real).05, 1 - beta.y());
+                    if (s.Get1D() < q) break;
+                    beta /= (Real)1 - q;
+                }
+            } else {
+                if (bounces == 0 && sc.envLight) L += sc.envLight->Le(r) * beta;
+                break;
+            }
+        }
+        return L;
+    }
+
+    /* DirectLightingIntegrator::Li (DirectLightingIntegrator.cpp:13-29) with SampleOneLight and
+     * EstimateDirect (Integrator.cpp:5-55), quirks kept; null surfaces crossed iteratively (256 at
+     * most); no environment light or no light: 0 (the reference dereferences null). */
+    Spec LiDirect(Ray r, Sampler &s) const {
+        RayHit hit;
+        for (int guard = 0; guard < 256; ++guard) {
+            if (!sc.Intersect(r, hit)) return sc.envLight ? sc.envLight->Le(r) : Spec(0);
+            const Material &m = Mat(hit);
+            if (m.bxdf < 0) { r.o = hit.point + r.d * (Real).0001; continue; }
+            ScatterEvent ev;
+            ev.hit = &hit;
+            ev.scene = &sc;
+            ev.wo = -r.d;
+            ev.SurfaceLocalise();
+            Real lightPdf = 1;
+            const LightBase *l = sc.lightSampler->Sample(ev, s, &lightPdf);
+            if (!l) return Spec(0);
+            Spec Ld(0);
+            Real scatteringPDF = 0, lightPDF = 0;
+            Spec Li = l->Sample_Li(ev, s, lightPDF);
+            if (lightPDF > 0 && !Li.IsBlack()) {
+                const Spec f = bx.f(m.bxdf, ev) * std::abs(ev.wiL.y);
+                scatteringPDF = bx.Pdf(m.bxdf, ev.woL, ev.wiL, ev);
+                if (!f.IsBlack() && scatteringPDF > 0) Ld += Li * f * PowerHeuristic(lightPDF, scatteringPDF) / lightPDF;
+            }
+            Spec f = bx.Sample_f(m.bxdf, ev, s, scatteringPDF);
+            f *= std::abs(ev.wiL.y);
+            if (scatteringPDF > 0 && !f.IsBlack()) {
+                lightPDF = l->PDF_Li(ev);
+                if (lightPDF == 0) return Ld / lightPdf;
+                const Real w = PowerHeuristic(scatteringPDF, lightPDF);
+                RayHit lh;
+                ScatterEvent be;
+                be.scene = &sc;
+                be.hit = &lh;
+                be.wo = -ev.wi;
+                const Ray br{hit.point + hit.normalG * (Real).00001, ev.wi};
+                Spec Lc(0);
+                if (sc.Intersect(br, lh)) {
+                    if (Mat(lh).light == l) Lc = Mat(lh).light->L(be);
+                } else {
+                    Lc = l->Le(br);
+                }
+                if (!Lc.IsBlack()) Ld += f * Lc * w / scatteringPDF;
+            }
+            return Ld / lightPdf;
+        }
+        return Spec(0);
+    }
+
+    /* NormalPass / DepthPass (UtilityIntegrators.cpp:7-53) as UtilityIntegrator::Li. */
+    Spec LiPass(Ray r, bool normal) const {
+        RayHit hit;
+        Real c[3];
+        if (sc.Intersect(r, hit)) {
+            if (normal) { c[0] = hit.normalS.x * (Real).5 + (Real).5; c[1] = hit.normalS.y * (Real).5 + 1; c[2] = hit.normalS.z * (Real).5 + (Real).5; }
+            else { const Real d = std::pow((hit.point - r.o).Magnitude() / (Real)100, (Real)1); c[0] = c[1] = c[2] = d; }
+        } else if (normal) { c[0] = c[1] = c[2] = 0; }
+        else { c[0] = 1; c[1] = 0; c[2] = 1; }
+        return FromRGB(c, false);
+    }
+
     /* MISVolumetricPathIntegrator::Li (MISVolumetricPathIntegrator.cpp:71-215) */
     Spec Li(Ray r, Sampler &s) const {
         Spec L(0), beta(1);
@@ -2277,7 +2516,15 @@ static Spec TracePath(const OracleRun &R, uint64_t pathId, Real rgbOut[3], uint3
     const V3 p = org + xh * (u * -tanFov2 + tanFov) + yh * (v * -tanFov2 * aspect + tanFov * aspect) + zh;
     Ray r{org, (p - org).Normalised()};
     Integrator I(R.o->sc, R.opt->max_bounces, R.opt->min_bounces);
-    const Spec L = I.Li(r, s);
+    Spec L;
+    switch (R.opt->integrator) {
+    case LGPU_INTEGRATOR_PATH: L = I.LiPath(r, s); break;
+    case LGPU_INTEGRATOR_VOLPATH: L = I.LiVolPath(r, s); break;
+    case LGPU_INTEGRATOR_DIRECT: L = I.LiDirect(r, s); break;
+    case LGPU_INTEGRATOR_NORMAL: L = I.LiPass(r, true); break;
+    case LGPU_INTEGRATOR_DEPTH: L = I.LiPass(r, false); break;
+    default: L = I.Li(r, s); break;
+    }
     if (dimsOut) *dimsOut = s.dim;
     if (g_ns == 3) { rgbOut[0] = L.c[0]; rgbOut[1] = L.c[1]; rgbOut[2] = L.c[2]; }
     else {

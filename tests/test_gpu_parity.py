@@ -114,3 +114,25 @@ def test_inverse_cornell_texture_medium_paths(gpu_lib, mode):
         frac, _ = path_agreement(g, o)
         assert np.isfinite(g).all()
         assert frac >= 0.99, "per-path agreement %.5f" % frac
+
+
+INTEGRATORS = pytest.mark.parametrize("integ", [0, 1, 2, 3, 4], ids=["path", "volpath", "direct", "normal", "depth"])
+
+
+@INTEGRATORS
+@pytest.mark.parametrize("scene", ["cornell", "volume", "terrain"])
+def test_other_integrators_paths(gpu_lib, integ, scene):
+    """PathIntegrator, VolumetricPathIntegrator, DirectLightingIntegrator and the normal / depth
+    passes (megakernel) against the oracle's restatements, per path."""
+    from lambda_gb300 import configs
+    if scene == "cornell":
+        sb, cam, opts = configs.cornell(32, 32, 4)
+    elif scene == "volume":
+        sb, cam, opts = configs.volume(32, 18, 4, max_depth=12, n_instances=40, sphere_res=(24, 24))
+    else:
+        sb, cam, opts = configs.terrain(32, 18, 4, grid=96, n_emitters=300)
+    opts.integrator = integ
+    g, o = _render_both(gpu_lib, sb, cam, opts, opts.width * opts.height * 4)
+    frac, _ = path_agreement(g, o)
+    assert np.isfinite(g).all()
+    assert frac >= 0.99, "per-path agreement %.5f" % frac
