@@ -519,14 +519,11 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
             const DObject &ob = objects[i];
             float inv[9];
             inverse3(ob.m, inv);
-            /* world -> object: x_obj = inv * (x - t) */
-            const float tx = -(inv[0] * ob.t[0] + inv[3] * ob.t[1] + inv[6] * ob.t[2]);
-            const float ty = -(inv[1] * ob.t[0] + inv[4] * ob.t[1] + inv[7] * ob.t[2]);
-            const float tz = -(inv[2] * ob.t[0] + inv[5] * ob.t[1] + inv[8] * ob.t[2]);
+            /* world -> object: x_obj = inv * (x - t); rows of inv, translation in w */
             DInst I;
-            I.r0 = make_float4(inv[0], inv[3], inv[6], tx);
-            I.r1 = make_float4(inv[1], inv[4], inv[7], ty);
-            I.r2 = make_float4(inv[2], inv[5], inv[8], tz);
+            I.r0 = make_float4(inv[0], inv[3], inv[6], ob.t[0]);
+            I.r1 = make_float4(inv[1], inv[4], inv[7], ob.t[1]);
+            I.r2 = make_float4(inv[2], inv[5], inv[8], ob.t[2]);
             I.root = blasRoot[o.mesh]; I.object = i; I.pad0 = I.pad1 = 0;
             insts.push_back(I);
             const lt::Box &b = objBox[i];

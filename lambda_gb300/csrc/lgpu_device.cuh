@@ -830,10 +830,14 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
             /* TLAS leaf: one instance record */
             const DInst *I = S.insts + ref;
             const float4 r0 = ldg4(&I->r0), r1 = ldg4(&I->r1), r2 = ldg4(&I->r2);
-            o = mk(r0.x * wo.x + r0.y * wo.y + r0.z * wo.z + r0.w, r1.x * wo.x + r1.y * wo.y + r1.z * wo.z + r1.w,
-                   r2.x * wo.x + r2.y * wo.y + r2.z * wo.z + r2.w);
-            d = mk(r0.x * wd.x + r0.y * wd.y + r0.z * wd.z, r1.x * wd.x + r1.y * wd.y + r1.z * wd.z,
-                   r2.x * wd.x + r2.y * wd.y + r2.z * wd.z);
+            /* inv * (o - t) and inv * d, unfused, in the order of the host's column-major product */
+            const float3 v = mk(__fsub_rn(wo.x, r0.w), __fsub_rn(wo.y, r1.w), __fsub_rn(wo.z, r2.w));
+            o = mk(add_rn(add_rn(mul_rn(r0.x, v.x), mul_rn(r0.y, v.y)), mul_rn(r0.z, v.z)),
+                   add_rn(add_rn(mul_rn(r1.x, v.x), mul_rn(r1.y, v.y)), mul_rn(r1.z, v.z)),
+                   add_rn(add_rn(mul_rn(r2.x, v.x), mul_rn(r2.y, v.y)), mul_rn(r2.z, v.z)));
+            d = mk(add_rn(add_rn(mul_rn(r0.x, wd.x), mul_rn(r0.y, wd.y)), mul_rn(r0.z, wd.z)),
+                   add_rn(add_rn(mul_rn(r1.x, wd.x), mul_rn(r1.y, wd.y)), mul_rn(r1.z, wd.z)),
+                   add_rn(add_rn(mul_rn(r2.x, wd.x), mul_rn(r2.y, wd.y)), mul_rn(r2.z, wd.z)));
             inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
             inst_obj = __ldg(&I->object);
             in_blas = true;

@@ -37,7 +37,8 @@ struct DTri {
 };
 
 struct DInst {
-    float4 r0, r1, r2;   /* world -> object affine rows */
+    float4 r0, r1, r2;   /* rows of the object's inverse linear part; w = the object's translation t
+                          * (world -> object: inv * (x - t)) */
     int root;            /* BLAS root node */
     int object;          /* object id written into hits (-1: per-triangle object ids) */
     int pad0, pad1;
