@@ -350,6 +350,17 @@ LGPU_API int lgpu_render_count(lgpu_context *ctx, const lgpu_camera_desc *camera
 LGPU_API int lgpu_intersect(lgpu_context *ctx, const float *rays_dev, uint32_t *hits_dev,
                             float *uv_out_dev, uint64_t n, void *stream);
 
+/* Film::ToRGBTexture (src/camera/Film.cpp:11-24) on the device: rgba_dev[i] = (film rgb / sample
+ * count, 1) for n_px float4 pixels (DEVICE buffers); pixels without samples give black. */
+LGPU_API int lgpu_film_resolve(const float *film_dev, float *rgba_dev, uint64_t n_px, void *stream);
+
+/* GPU counterpart of ProgressiveRender::RunPass (src/render/ProgressiveRender.cpp:40-58): `passes`
+ * renders of opts->spp samples per pixel, each with the next opts->spp sample indices
+ * (sample_offset advanced per pass), added into the DEVICE film; after every pass the film is
+ * resolved into rgba_dev (optional) as UpdateOutputTexture does.  Returns when done. */
+LGPU_API int lgpu_render_progressive(lgpu_context *ctx, const lgpu_camera_desc *camera, const lgpu_render_opts *opts,
+                                     int32_t passes, float *film_dev, float *rgba_dev, void *stream);
+
 /* One view of a batched render: a camera with its own film size, samples per pixel, depth and seed.
  * film_dev is the view's DEVICE film (width * height float4: r, g, b, sample count), which the render
  * adds into as Film::AddSample does (src/camera/Film.h:30-33). */

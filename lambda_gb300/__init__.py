@@ -17,7 +17,8 @@ LIB_PATH = HERE / "_build" / "liblambda_gpu.so"
 
 EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_scene_commit", "lgpu_render",
            "lgpu_render_device", "lgpu_render_paths", "lgpu_render_count", "lgpu_intersect",
-           "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc", "lgpu_render_batch", "lgpu_autotune", "lgpu_adjoint"]
+           "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc", "lgpu_render_batch", "lgpu_autotune", "lgpu_adjoint", "lgpu_film_resolve",
+           "lgpu_render_progressive"]
 
 _lib = None
 
@@ -58,6 +59,9 @@ def lib():
         L.lgpu_render_batch.argtypes = [vp, C.POINTER(abi.ViewDesc), C.c_int32, C.POINTER(abi.RenderOpts), vp]
         L.lgpu_adjoint.argtypes = [vp, C.POINTER(abi.CameraDesc), C.POINTER(abi.RenderOpts),
                                    C.POINTER(abi.AdjointDesc), vp, vp, vp, vp]
+        L.lgpu_film_resolve.argtypes = [vp, vp, C.c_uint64, vp]
+        L.lgpu_render_progressive.argtypes = [vp, C.POINTER(abi.CameraDesc), C.POINTER(abi.RenderOpts), C.c_int32,
+                                              vp, vp, vp]
         L.lgpu_autotune.argtypes = [vp, C.POINTER(abi.ViewDesc), C.c_int32, C.POINTER(abi.RenderOpts), C.c_int32,
                                     C.POINTER(abi.Tuning)]
         _lib = L
@@ -159,6 +163,13 @@ class Renderer:
         self._check(lib().lgpu_adjoint(self._h, C.byref(cam), C.byref(opts), C.byref(p), C.c_void_p(dloss_ptr),
                                        C.c_void_p(grad_tex_ptr) if grad_tex_ptr else None,
                                        C.c_void_p(grad_scalars_ptr), C.c_void_p(stream) if stream else None))
+
+    def render_progressive(self, camera, opts, passes, film_ptr, rgba_ptr=None, stream=None):
+        """lgpu_render_progressive: passes of opts.spp samples into a device film, resolved to rgba."""
+        cam = camera.desc()
+        self._check(lib().lgpu_render_progressive(self._h, C.byref(cam), C.byref(opts), passes, C.c_void_p(film_ptr),
+                                                  C.c_void_p(rgba_ptr) if rgba_ptr else None,
+                                                  C.c_void_p(stream) if stream else None))
 
     def render_count(self, camera, opts):
         cam = camera.desc()

@@ -1327,6 +1327,40 @@ LGPU_API int lgpu_intersect(lgpu_context *c, const float *rays_dev, uint32_t *hi
 
 }  // extern "C"
 
+/* ------------------------------------------------------------------ progressive passes, film output */
+extern "C" {
+
+LGPU_API int lgpu_film_resolve(const float *film_dev, float *rgba_dev, uint64_t n_px, void *stream) {
+    if (!film_dev || !rgba_dev) return LGPU_ERR_INVALID_ARG;
+    cudaError_t e = film_resolve(reinterpret_cast<const float4 *>(film_dev), reinterpret_cast<float4 *>(rgba_dev), n_px,
+                                 (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    return e == cudaSuccess ? LGPU_OK : LGPU_ERR_CUDA;
+}
+
+LGPU_API int lgpu_render_progressive(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o,
+                                     int32_t passes, float *film_dev, float *rgba_dev, void *stream) {
+    int r = check_opts(c, cam, o);
+    if (r) return r;
+    if (passes < 0 || !film_dev) return fail(c, LGPU_ERR_INVALID_ARG, "bad progressive pass arguments");
+    cudaSetDevice(c->device);
+    const uint64_t n = (uint64_t)o->width * o->height * o->spp;
+    lgpu_render_opts po = *o;
+    for (int p = 0; p < passes; ++p) {
+        po.sample_offset = o->sample_offset + (uint32_t)(p * o->spp);   /* the next o->spp samples of every pixel */
+        r = render_impl(c, cam, &po, reinterpret_cast<float4 *>(film_dev), nullptr, nullptr, n, false, (cudaStream_t)stream);
+        if (r) return r;
+        if (rgba_dev) {   /* ProgressiveRender::UpdateOutputTexture after each pass */
+            cudaError_t e = film_resolve(reinterpret_cast<const float4 *>(film_dev), reinterpret_cast<float4 *>(rgba_dev),
+                                         (uint64_t)o->width * o->height, (cudaStream_t)stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "film resolve");
+        }
+    }
+    return finish_timing(c);
+}
+
+}  // extern "C"
+
 /* ------------------------------------------------------------------ batched views
  *
  * lgpu_render_batch renders many views of the committed scene -- each with its own camera, film

@@ -431,6 +431,19 @@ __global__ void k_film_reduce(const float4 *paths, float4 *film, uint64_t first_
     f.x += r; f.y += g; f.z += b; f.w += (float)spp;
     film[first_px + p] = f;
 }
+/* Film::ToRGBTexture (src/camera/Film.cpp:11-24): rgba = (spectrum / nSamples, 1); a pixel
+ * without samples resolves to black instead of the reference's division by zero. */
+__global__ void k_film_resolve(const float4 *film, float4 *rgba, uint64_t n_px) {
+    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_px) return;
+    const float4 f = film[p];
+    rgba[p] = f.w > 0.f ? make_float4(f.x / f.w, f.y / f.w, f.z / f.w, 1.f) : make_float4(0.f, 0.f, 0.f, 1.f);
+}
+cudaError_t film_resolve(const float4 *film, float4 *rgba, uint64_t n_px, cudaStream_t st) {
+    if (n_px == 0) return cudaSuccess;
+    k_film_resolve<<<(unsigned)((n_px + 255) / 256), 256, 0, st>>>(film, rgba, n_px);
+    return cudaGetLastError();
+}
 cudaError_t film_reduce(const float4 *paths, float4 *film, uint64_t first_px, uint64_t n_px, int spp, cudaStream_t st) {
     if (n_px == 0) return cudaSuccess;
     k_film_reduce<<<(unsigned)((n_px + 255) / 256), 256, 0, st>>>(paths, film, first_px, n_px, spp);
