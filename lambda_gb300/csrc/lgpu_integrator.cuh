@@ -280,6 +280,40 @@ struct Tracer {
         }
         return distSq / (cT * area);
     }
+    /* Light::PDF_Li(event, sampler): the pdf of direction ev.wi from the shading point h, found
+     * with a ray query -- MeshLight.cpp:43-54 (no triangle-selection factor; TriangleLight delegates
+     * to its mesh light, :153-155), EnvironmentLight.cpp:47-58 (the ray must escape), 0 for delta
+     * lights.  Used by DirectLightingIntegrator's BSDF-sampled strategy. */
+    __device__ __noinline__ float pdf_li_dir(LRef r, const Event &ev, const RayHit &h) {
+        if (r.light < 0) return 0.f;
+        const DLight &L = S.lights[r.light];
+        if (L.type == LT_ENV) {
+            const DEnv &E = S.env;
+            const float theta = spherical_theta(ev.wi) - E.offy;
+            const float phi = spherical_phi(ev.wi) - E.offx;
+            const float sT = sinf(theta);
+            if (sT == 0.f) return 0.f;
+            const float3 wOff = spherical_dir(sT, cosf(theta), phi);
+            if (!ray_escapes(h.point, wOff, ev, nullptr)) return 0.f;
+            const float u = fractf(phi * INV_PI2), v = fractf(theta * INV_PI);
+            const int iu = max(min((int)(u * (float)E.w), E.w - 1), 0);
+            const int iv = max(min((int)(v * (float)E.h), E.h - 1), 0);
+            const int co = E.cond_off + iv * (2 * E.w + 2);
+            return S.fpool[co + E.w + 1 + iu] / E.marg_integral / (2.f * PI * PI * sT);
+        }
+        if (L.type != LT_MESH) return 0.f;
+        const float3 o = h.point + h.nG * (SURFACE_EPSILON * (float)ev.sidedness);
+        RayHit hh;
+        hh.tFar = finf(); hh.uv = make_float2(0.f, 0.f);
+        const bool hit = S.has_volumes ? intersect_tr(o, ev.wi, hh, ev.medium, nullptr, -1.f) : intersect(o, ev.wi, hh);
+        if (!hit || mat(hh).light != r.light || hh.prim >= L.num_tris) return 0.f;
+        float3 a, b, c, n;
+        tri_verts(L, hh.prim, a, b, c);
+        float area;
+        area_normal(a, b, c, &area, &n);
+        const float cT = fabsf(dot(n, -ev.wi));
+        return cT > 0.f ? distsq(h.point, hh.point) / (cT * area) : 0.f;
+    }
     /* Light::SamplePoint (MeshLight.cpp:55-70, :167-181, PointLight.cpp:40-44). */
     __device__ __noinline__ Spec<NS> sample_point(LRef r, Event &ev, RayHit &h, float3 &lpoint, float3 &lnormal, float &lpdf) {
         if (r.light < 0) { lpdf = 0.f; lpoint = h.point; return Spec<NS>(0.f); }
@@ -710,9 +744,11 @@ struct Tracer {
 
     /* DirectLightingIntegrator::Li (src/integrators/DirectLightingIntegrator.cpp:13-29) with
      * Integrator::SampleOneLight / EstimateDirect (src/integrators/Integrator.cpp:5-55).  The
-     * reference's quirks are kept: the BSDF-sampled light pdf is PDF_Li at the shading point, and
-     * the BSDF-sampled hit counts only if its light is the sampled light object itself.  Null surfaces
-     * are crossed with a 1e-4 offset (at most 256 times); an absent environment light gives 0. */
+     * reference's quirks are kept: the BSDF-sampled light pdf is PDF_Li(event, sampler) (a ray query
+     * from the shading point, without the mesh's triangle-selection factor), and the BSDF-sampled
+     * hit counts only if its light is the sampled light object itself.  Null surfaces
+     * are crossed with a 1e-4 offset (at most 256 times); an absent environment light gives 0, so does
+     * a light-selection pdf that is not positive (the reference divides by it). */
     __device__ Spec<NS> Li_direct(float3 ro, float3 rd) {
         RayHit hit;
         hit.tFar = finf(); hit.uv = make_float2(0.f, 0.f);
@@ -729,6 +765,7 @@ struct Tracer {
             float lightPdf = 1.f;
             const LRef l = sample_light(hit.point, hit.nS, &lightPdf);
             if (l.light < 0) return Spec<NS>(0.f);
+            const bool pdfOk = lightPdf > 0.f;   /* a zero or NaN selection pdf would make the estimate NaN */
             /* EstimateDirect */
             Spec<NS> Ld(0.f);
             float scatteringPDF = 0.f, lightPDF = 0.f;
@@ -741,8 +778,8 @@ struct Tracer {
             Spec<NS> f = bsdf_sample<NS>(b, ev, hit, rng, scatteringPDF);   /* moves hit.point off the surface */
             f *= fabsf(ev.wiL.y);
             if (scatteringPDF > 0.f && !f.black()) {
-                lightPDF = pdf_li(l, ev, hit);
-                if (lightPDF == 0.f) return Ld / lightPdf;
+                lightPDF = pdf_li_dir(l, ev, hit);
+                if (lightPDF == 0.f) return pdfOk ? Ld / lightPdf : Spec<NS>(0.f);
                 const float w = power_heuristic(scatteringPDF, lightPDF);
                 const float3 o2 = hit.point + hit.nG * .00001f;
                 RayHit lh;
@@ -760,7 +797,7 @@ struct Tracer {
                 }
                 if (!Lc.black()) Ld += f * Lc * w / scatteringPDF;
             }
-            return Ld / lightPdf;
+            return pdfOk ? Ld / lightPdf : Spec<NS>(0.f);
         }
         return Spec<NS>(0.f);
     }

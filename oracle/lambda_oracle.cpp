@@ -1120,6 +1120,9 @@ struct LightBase {
     virtual ~LightBase() {}
     virtual Spec Sample_Li(ScatterEvent &ev, Sampler &s, Real &pdf) const = 0;
     virtual Real PDF_Li(const ScatterEvent &ev) const = 0;
+    /* Light::PDF_Li(event, sampler): the pdf of direction ev.wi from the shading point, found with
+     * a ray query (EstimateDirect's BSDF-sampled strategy); 0 for delta lights */
+    virtual Real PDF_Li_S(const ScatterEvent &, Sampler &) const { return 0; }
     virtual Spec SamplePoint(Sampler &s, ScatterEvent &ev, PartialLightSample *ls) const = 0;
     virtual Spec Visibility(const V3 &p, ScatterEvent &ev, Sampler &s, PartialLightSample *ls) const = 0;
     virtual Spec Le(const Ray &) const { return Spec(0); }
@@ -1411,6 +1414,7 @@ struct TriangleLight : LightBase {
     TriangleLight(const MeshLight *m, unsigned i) : ml(m), tri(i) {}
     Spec Sample_Li(ScatterEvent &ev, Sampler &s, Real &pdf) const override;
     Real PDF_Li(const ScatterEvent &ev) const override;
+    Real PDF_Li_S(const ScatterEvent &ev, Sampler &s) const override;
     Spec SamplePoint(Sampler &s, ScatterEvent &ev, PartialLightSample *ls) const override;
     Spec Visibility(const V3 &p, ScatterEvent &ev, Sampler &s, PartialLightSample *ls) const override;
     Spec L(const ScatterEvent &ev) const override;
@@ -1450,6 +1454,19 @@ struct MeshLight : LightBase {   /* MeshLight.cpp:1-125 */
         }
         pdf = 0;
         return Spec(0);
+    }
+    /* MeshLight::PDF_Li(event, sampler) (MeshLight.cpp:43-54): no triangle-selection factor */
+    Real PDF_Li_S(const ScatterEvent &ev, Sampler &s) const override {
+        RayHit h;
+        const Ray r{ev.hit->point + ev.hit->normalG * SURFACE_EPSILON * (Real)ev.sidedness, ev.wi};
+        const bool hit = sc->hasVolumes ? sc->IntersectTr(r, h, s, ev.medium, nullptr) : sc->Intersect(r, h);
+        if (!hit) return 0;
+        if (sc->materials[h.object->material].light != this) return 0;
+        Real area; V3 n;
+        mesh->GetAreaNormal(h.primId, &area, &n);
+        const Real cosT = std::abs(Dot(n, -ev.wi));
+        if (cosT > 0) return DistSq(ev.hit->point, h.point) / (cosT * area);
+        return 0;
     }
     Real PDF_Li(const ScatterEvent &ev) const override {
         if (Dot(ev.wi, ev.hit->normalG) > 0) return 0;
@@ -1507,6 +1524,8 @@ Spec TriangleLight::Sample_Li(ScatterEvent &ev, Sampler &s, Real &pdf) const {
     pdf = 0;
     return Spec(0);
 }
+/* TriangleLight::PDF_Li(event, sampler) (MeshLight.cpp:153-155) */
+Real TriangleLight::PDF_Li_S(const ScatterEvent &ev, Sampler &s) const { return ml->PDF_Li_S(ev, s); }
 Real TriangleLight::PDF_Li(const ScatterEvent &ev) const {
     if (Dot(ev.wi, ev.hit->normalG) > 0) return 0;
     const Real distSq = ev.hit->tFar * ev.hit->tFar;
@@ -1684,6 +1703,17 @@ struct EnvLightO : LightBase {   /* EnvironmentLight.cpp:7-108 */
         const Real sinT = std::sin(theta);
         if (sinT == 0) return 0;
         return dist.PDF(V2(Fract(phi * INV_PI2), Fract(theta * INV_PI))) / ((Real)2 * PI * PI * sinT);
+    }
+    /* EnvironmentLight::PDF_Li(event, sampler) (EnvironmentLight.cpp:47-58) */
+    Real PDF_Li_S(const ScatterEvent &ev, Sampler &s) const override {
+        const Real theta = SphericalTheta(ev.wi) - offset.y;
+        const Real phi = SphericalPhi(ev.wi) - offset.x;
+        const Real sinT = std::sin(theta);
+        if (sinT == 0) return 0;
+        const V3 wOff = SphericalDirection(sinT, std::cos(theta), phi);
+        if (LRayEscapes(Ray{ev.hit->point, wOff}, ev, s, nullptr))
+            return dist.PDF(V2(Fract(phi * INV_PI2), Fract(theta * INV_PI))) / ((Real)2 * PI * PI * sinT);
+        return 0;
     }
     Spec SamplePoint(Sampler &, ScatterEvent &, PartialLightSample *ls) const override { ls->pdf *= 0; ls->point = V3(0, 0, 0); return Spec(0); }
     Spec Visibility(const V3 &sp, ScatterEvent &ev, Sampler &s, PartialLightSample *ls) const override {
@@ -2153,7 +2183,8 @@ struct Integrator {
 
     /* DirectLightingIntegrator::Li (DirectLightingIntegrator.cpp:13-29) with SampleOneLight and
      * EstimateDirect (Integrator.cpp:5-55), quirks kept; null surfaces crossed iteratively (256 at
-     * most); no environment light or no light: 0 (the reference dereferences null). */
+     * most); no environment light or no light: 0 (the reference dereferences null); a light-selection
+     * pdf that is not positive gives 0 (the reference divides by it). */
     Spec LiDirect(Ray r, Sampler &s) const {
         RayHit hit;
         for (int guard = 0; guard < 256; ++guard) {
@@ -2168,6 +2199,7 @@ struct Integrator {
             Real lightPdf = 1;
             const LightBase *l = sc.lightSampler->Sample(ev, s, &lightPdf);
             if (!l) return Spec(0);
+            const bool pdfOk = lightPdf > 0;   /* a zero or NaN selection pdf would make the estimate NaN */
             Spec Ld(0);
             Real scatteringPDF = 0, lightPDF = 0;
             Spec Li = l->Sample_Li(ev, s, lightPDF);
@@ -2179,8 +2211,8 @@ struct Integrator {
             Spec f = bx.Sample_f(m.bxdf, ev, s, scatteringPDF);
             f *= std::abs(ev.wiL.y);
             if (scatteringPDF > 0 && !f.IsBlack()) {
-                lightPDF = l->PDF_Li(ev);
-                if (lightPDF == 0) return Ld / lightPdf;
+                lightPDF = l->PDF_Li_S(ev, s);
+                if (lightPDF == 0) return pdfOk ? Ld / lightPdf : Spec(0);
                 const Real w = PowerHeuristic(scatteringPDF, lightPDF);
                 RayHit lh;
                 ScatterEvent be;
@@ -2196,7 +2228,7 @@ struct Integrator {
                 }
                 if (!Lc.IsBlack()) Ld += f * Lc * w / scatteringPDF;
             }
-            return Ld / lightPdf;
+            return pdfOk ? Ld / lightPdf : Spec(0);
         }
         return Spec(0);
     }
