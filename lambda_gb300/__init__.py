@@ -5,6 +5,7 @@ include/lambda_gpu.h); this module only binds it with ctypes.  There is no CPU f
 library or a GPU is missing, every entry point raises.
 """
 import ctypes as C
+import os
 import pathlib
 
 import numpy as np
@@ -13,7 +14,7 @@ from . import abi
 from .scene import Camera, SceneBuilder, out  # noqa: F401
 
 HERE = pathlib.Path(__file__).resolve().parent
-LIB_PATH = HERE / "_build" / "liblambda_gpu.so"
+LIB_PATH = pathlib.Path(os.environ["LGPU_LIB_PATH"]) if os.environ.get("LGPU_LIB_PATH") else HERE / "_build" / "liblambda_gpu.so"
 
 EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_scene_commit", "lgpu_render",
            "lgpu_render_device", "lgpu_render_paths", "lgpu_render_count", "lgpu_intersect",
@@ -30,6 +31,9 @@ class LambdaGPUError(RuntimeError):
 
 
 def build(force=False):
+    """Build the extension in-tree (a no-op when LGPU_LIB_PATH selects a prebuilt tuning variant)."""
+    if os.environ.get("LGPU_LIB_PATH"):
+        return LIB_PATH
     from .build_ext import build as _b
     return _b(force=force)
 

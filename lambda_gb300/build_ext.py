@@ -34,17 +34,21 @@ def _flags():
             "-I" + str(CSRC), "-I" + str(HERE.parent / "include")]
 
 
-def build(force=False, verbose=False):
-    OUT.mkdir(parents=True, exist_ok=True)
+def build(force=False, verbose=False, defines=(), out_dir=None):
+    """Compile into lambda_gb300/_build (or out_dir, for tuning variants built with extra
+    -D defines such as LGPU_RESUME_MINB=5 or LGPU_NO_STAGE)."""
+    out = pathlib.Path(out_dir) if out_dir else OUT
+    lib_path = out / LIB.name
+    out.mkdir(parents=True, exist_ok=True)
     deps = list(CSRC.glob("*")) + [HERE.parent / "include" / "lambda_gpu.h"]
     newest = max(p.stat().st_mtime for p in deps)
-    if LIB.exists() and not force and LIB.stat().st_mtime >= newest:
-        return LIB
+    if lib_path.exists() and not force and lib_path.stat().st_mtime >= newest:
+        return lib_path
 
     def compile_one(spec):
         src, defs, name = spec
-        obj = OUT / (name + ".o")
-        cmd = [nvcc(), *_flags(), *defs, "-c", str(CSRC / src), "-o", str(obj)]
+        obj = out / (name + ".o")
+        cmd = [nvcc(), *_flags(), *defs, *["-D" + d for d in defines], "-c", str(CSRC / src), "-o", str(obj)]
         if verbose and src.endswith(".cu"):
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -58,13 +62,13 @@ def build(force=False, verbose=False):
     if verbose:
         for _, log in results:
             print(log)
-    tmp = LIB.with_suffix(".so.tmp%d" % os.getpid())
+    tmp = lib_path.with_suffix(".so.tmp%d" % os.getpid())
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -231,8 +231,24 @@ __device__ __forceinline__ void warp_stage(PHot<NS> *G, PHot<NS> *sh, int slot, 
  * a launch sized to the queue runs the loop body once per thread; a device-driven launch (fixed
  * grid, n read from W.count_in) loops.  The loop bound is block-uniform, so warps stay converged
  * for the warp-cooperative staging. */
+/* Build-time tuning knobs (defaults are the measured best on the 1080p terrain):
+ * LGPU_RESUME_MINB: minimum resident blocks per SM requested from the compiler for resume/spawn;
+ * LGPU_NO_STAGE: path states are used in place in HBM instead of staged through shared memory. */
+#ifndef LGPU_RESUME_MINB
+#define LGPU_RESUME_BOUNDS __launch_bounds__(128)
+#else
+#define LGPU_RESUME_BOUNDS __launch_bounds__(128, LGPU_RESUME_MINB)
+#endif
+#ifdef LGPU_NO_STAGE
+#define LG_STAGE(G, sh, slot, in)
+#define LG_STATE(G, sh, slot) (G[slot])
+#else
+#define LG_STAGE(G, sh, slot, in) warp_stage<NS>(G, sh, slot, in)
+#define LG_STATE(G, sh, slot) (sh[threadIdx.x & 31])
+#endif
+
 template <int NS, bool COUNT, bool DEV>
-__global__ void __launch_bounds__(128) k_wave_resume(const __grid_constant__ WaveArgs W, int n) {
+__global__ void LGPU_RESUME_BOUNDS k_wave_resume(const __grid_constant__ WaveArgs W, int n) {
     extern __shared__ float4 smem4[];
     if (DEV) n = W.count_in[W.seg_sel];
     PHot<NS> *G = reinterpret_cast<PHot<NS> *>(W.states);
@@ -251,10 +267,10 @@ __global__ void __launch_bounds__(128) k_wave_resume(const __grid_constant__ Wav
                 slot = W.queue_in[seg * W.cap_in + (i - W.seg_off[seg])];
             }
         }
-        warp_stage<NS>(G, sh, slot, true);
+        LG_STAGE(G, sh, slot, true);
         int keep = -1;
         if (slot >= 0) {
-            PHot<NS> &s = sh[threadIdx.x & 31];
+            PHot<NS> &s = LG_STATE(G, sh, slot);
             PCold<NS> &c = reinterpret_cast<PCold<NS> *>(W.cold)[slot];
             Wave<NS, COUNT> w{W, s, c, slot};
             w.rng.key = s.key;
@@ -266,7 +282,7 @@ __global__ void __launch_bounds__(128) k_wave_resume(const __grid_constant__ Wav
             else { wave_save(w, s); keep = slot; }
         }
         __syncwarp();
-        warp_stage<NS>(G, sh, keep, false);
+        LG_STAGE(G, sh, keep, false);
     }
 }
 
@@ -274,7 +290,7 @@ __global__ void __launch_bounds__(128) k_wave_resume(const __grid_constant__ Wav
  * warps of a spawn trace neighbouring samples of one pixel.  Slots come from the free list, or from
  * the untouched tail of the pool on the first spawn.  Grid-stride like k_wave_resume. */
 template <int NS, bool COUNT, bool DEV>
-__global__ void __launch_bounds__(128) k_wave_spawn(const __grid_constant__ WaveArgs W, int n_max, int fresh) {
+__global__ void LGPU_RESUME_BOUNDS k_wave_spawn(const __grid_constant__ WaveArgs W, int n_max, int fresh) {
     extern __shared__ float4 smem4[];
     const int nfree = fresh ? n_max : *W.free_count;
     const unsigned long long next = *W.next_path;
@@ -288,7 +304,7 @@ __global__ void __launch_bounds__(128) k_wave_spawn(const __grid_constant__ Wave
         int keep = -1;
         if (i < m) {
             const int slot = fresh ? i : W.free_list[i];
-            PHot<NS> &s = sh[threadIdx.x & 31];
+            PHot<NS> &s = LG_STATE(G, sh, slot);
             PCold<NS> &c = reinterpret_cast<PCold<NS> *>(W.cold)[slot];
             Wave<NS, COUNT> w{W, s, c, slot};
             w.start_path(next + (uint64_t)i);
@@ -297,7 +313,7 @@ __global__ void __launch_bounds__(128) k_wave_spawn(const __grid_constant__ Wave
             else { wave_save(w, s); keep = slot; }
         }
         __syncwarp();
-        warp_stage<NS>(G, sh, keep, false);
+        LG_STAGE(G, sh, keep, false);
     }
 }
 /* next_path += paths started by the last spawn; clear the free list. */
@@ -322,7 +338,11 @@ static int resident_grid(K kernel, int block, size_t smem) {
 
 cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, int start_new, cudaStream_t st) {
     constexpr bool C = LGPU_COUNT != 0;
+#ifdef LGPU_NO_STAGE
+    const size_t smem = 0;
+#else
     const size_t smem = 128 * sizeof(PHot<LGPU_NS>);
+#endif
     static int grid_resume = 0, grid_spawn = 0;
     if (!grid_resume) {
         for (auto k : {k_wave_resume<LGPU_NS, C, false>, k_wave_resume<LGPU_NS, C, true>})
