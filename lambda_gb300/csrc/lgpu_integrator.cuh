@@ -827,6 +827,12 @@ struct Tracer {
      * The reference's MIS weights do not always sum to one over the strategies (its light pdf for
      * a BSDF-sampled hit is the mesh light's, the sampled one the triangle's), so the weights are
      * differentiated too: d ln w of the power heuristic through the parameter-dependent pdf.
+     * The reference also drops a surface vertex's light-sampled estimate when the BSDF sample
+     * that follows it fails (a microfacet reflection below the horizon ends the path before the
+     * estimate is added), so that estimate's expectation is scaled by the probability P(alpha)
+     * of a valid BSDF sample.  Its derivative dP = integral over valid directions of dp/dalpha is
+     * estimated on the same sample by (dp/dalpha) / p of the sampled direction, added to the
+     * light-sampled estimate's log-derivative.
      * Parameters: texels of an image-texture albedo (Lambertian, linear), the roughness of one
      * material's first BSDF leaf (central difference of the BSDF value), the grey sigma_a and
      * sigma_s of one homogeneous medium (transmittance exp(-sigma_t len) and the sigma_s factor of
@@ -1075,7 +1081,9 @@ struct Tracer {
                         } else break;
                         const Spec<NS> CN = beta * LdN, CS = beta * LdS;
                         L += CN + CS;
-                        credit(A, E, ne, CN, dl, Dr + DrN, Dsa + Spec<NS>(-lenN), Dss + Spec<NS>(-lenN), g);
+                        /* dpS / pS: score of the BSDF sample's validity, which keeps the light estimate */
+                        credit(A, E, ne, CN, dl, Dr + DrN + Spec<NS>(dpS / scatteringPDF), Dsa + Spec<NS>(-lenN),
+                               Dss + Spec<NS>(-lenN), g);
                         credit(A, E, ne, CS, dl, Dr + DrS + DwS, Dsa, Dss, g);
                         beta *= f / scatteringPDF;
                         Dr += DrS;

@@ -7,12 +7,12 @@ difference re-renders with the same seed at theta +- eps.
 * Albedo texture: without Russian roulette the albedo moves no sampling decision, so the difference
   is the derivative of the same estimator and must match to 1e-3 (eps = 1e-3); with roulette the
   two agree within 3 % at 2048 spp (eps = 1e-2).
-* Medium sigma_a, sigma_s and GGX roughness move sampling decisions (distance and microfacet
-  sampling).  The replay holds them fixed, which is the derivative of the estimator's expectation
-  only where that estimator is unbiased for every parameter value; the reference's estimator keeps
-  quirks (equiangular sampling measured from the perpendicular foot, the scattering-form weight on
-  pass-through segments, mesh- versus triangle-light pdfs in MIS) that it is not, so these gradients
-  are checked for sign and magnitude (25 %) only; the measured gaps are recorded in the design notes.
+* GGX roughness moves the microfacet sample; the replay holds it fixed and adds the score of the
+  sample's validity (the reference drops a vertex's light-sampled estimate when the reflected
+  direction falls below the horizon, with a probability that changes with roughness).  Checked to
+  5 % (measured 0.01 % at this seed; the difference itself varies by about 2 % across seeds).
+* Medium sigma_a and sigma_s move the distance sample; the difference is noisier here (it moved by
+  15 % across seeds at 2048 spp while the adjoint moved by 1 %), so these are checked to 15 %.
 """
 import numpy as np
 import pytest
@@ -25,7 +25,7 @@ SPP_EXACT = 512
 EPS = 1e-2
 EPS_EXACT = 1e-3
 TOL = 0.03
-TOL_SCALAR = 0.25
+TOL_SCALAR = {"roughness": 0.05, "sigma_a": 0.15, "sigma_s": 0.15}
 CAM = 3
 
 
@@ -110,7 +110,7 @@ def test_adjoint_scalars(setup, gpu_lib, name, idx):
     gsc = setup[5]
     fd = _fd(setup, gpu_lib, **{name: 1.0})
     assert np.isfinite(gsc[idx]) and np.sign(gsc[idx]) == np.sign(fd), (name, gsc[idx], fd)
-    assert abs(gsc[idx] - fd) <= TOL_SCALAR * abs(fd), (name, gsc[idx], fd)
+    assert abs(gsc[idx] - fd) <= TOL_SCALAR[name] * abs(fd), (name, gsc[idx], fd)
 
 
 def test_adjoint_rejects_hero_mode(gpu_lib):
