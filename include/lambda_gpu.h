@@ -219,6 +219,10 @@ typedef struct lgpu_medium_desc {
 typedef struct lgpu_texture_desc {
     const float *rgba;
     int32_t width, height;
+    int32_t aperture_mask;    /* nonzero: also build the sampling distribution of |red| that a masked
+                               * aperture over this texture draws from (MaskedAperture::InitDistribution,
+                               * src/camera/Aperture.cpp:38-51), at scene commit */
+    int32_t pad;
 } lgpu_texture_desc;
 
 typedef struct lgpu_scene_desc {
@@ -233,15 +237,34 @@ typedef struct lgpu_scene_desc {
     const lgpu_texture_desc *textures; int32_t num_textures;
 } lgpu_scene_desc;
 
-/* Pinhole camera (src/camera/Camera.cpp:7-44): origin, the three axes and the field of view.
- * aspect = height / width as in Camera::Camera. */
+/* Cameras (src/camera/Camera.cpp:7-71) and apertures (src/camera/Aperture.cpp:10-51): origin, the
+ * three axes and the field of view; aspect = height / width as in Camera::Camera.  A sample's
+ * random numbers: pixel jitter x, y (Render.cpp:55-56), then the aperture's (blade: one for the
+ * blade, two for the point; circular and masked: two), then the integrator's. */
+typedef enum lgpu_camera_type {
+    LGPU_CAMERA_PINHOLE = 0,      /* PinholeCamera::GenerateRay (Camera.cpp:41-44) */
+    LGPU_CAMERA_THIN_LENS = 1,    /* ThinLensCamera::GenerateRay (Camera.cpp:53-58) */
+    LGPU_CAMERA_SPHERICAL = 2     /* SphericalCamera::GenerateRay (Camera.cpp:66-71) */
+} lgpu_camera_type;
+typedef enum lgpu_aperture_type {
+    LGPU_APERTURE_NONE = 0,       /* thin lens without an aperture: ap = (0, 0), no random numbers */
+    LGPU_APERTURE_CIRCULAR = 1,   /* CircularAperture::Sample_p (Aperture.cpp:25-27) */
+    LGPU_APERTURE_BLADE = 2,      /* BladeAperture::Sample_p (Aperture.cpp:10-19) */
+    LGPU_APERTURE_MASKED = 3      /* MaskedAperture::Sample_p (Aperture.cpp:33-36) */
+} lgpu_aperture_type;
 typedef struct lgpu_camera_desc {
     float origin[3];
     float x_hat[3];
     float y_hat[3];
     float z_hat[3];
     float fov;
-    int32_t type;             /* 0 = pinhole */
+    int32_t type;             /* lgpu_camera_type */
+    float focal_length;       /* thin lens: ThinLensCamera::focalLength (the C API's default is 1) */
+    int32_t aperture;         /* thin lens: lgpu_aperture_type (the C API's default: circular, size 0) */
+    float aperture_size;      /* Aperture::size */
+    int32_t blades;           /* BladeAperture::blades (>= 3) */
+    int32_t aperture_mask;    /* masked: index of a scene texture committed with aperture_mask set */
+    float offset_phi, offset_theta;   /* spherical: SphericalCamera::offsetPhi / offsetTheta */
 } lgpu_camera_desc;
 
 /* RenderDirective fields (src/render/Render.h:12-20) plus the GPU-side knobs. */

@@ -60,7 +60,8 @@ class MediumDesc(C.Structure):
 
 
 class TextureDesc(C.Structure):
-    _fields_ = [("rgba", F32P), ("width", C.c_int32), ("height", C.c_int32)]
+    _fields_ = [("rgba", F32P), ("width", C.c_int32), ("height", C.c_int32), ("aperture_mask", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 class SceneDesc(C.Structure):
@@ -74,9 +75,16 @@ class SceneDesc(C.Structure):
                 ("textures", C.POINTER(TextureDesc)), ("num_textures", C.c_int32)]
 
 
+CAMERA_PINHOLE, CAMERA_THIN_LENS, CAMERA_SPHERICAL = 0, 1, 2
+APERTURE_NONE, APERTURE_CIRCULAR, APERTURE_BLADE, APERTURE_MASKED = 0, 1, 2, 3
+
+
 class CameraDesc(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("x_hat", C.c_float * 3), ("y_hat", C.c_float * 3),
-                ("z_hat", C.c_float * 3), ("fov", C.c_float), ("type", C.c_int32)]
+                ("z_hat", C.c_float * 3), ("fov", C.c_float), ("type", C.c_int32),
+                ("focal_length", C.c_float), ("aperture", C.c_int32), ("aperture_size", C.c_float),
+                ("blades", C.c_int32), ("aperture_mask", C.c_int32), ("offset_phi", C.c_float),
+                ("offset_theta", C.c_float)]
 
 
 class ViewDesc(C.Structure):

@@ -41,6 +41,8 @@ struct lgpu_context {
     bool have_scene = false;
     lgpu_stats stats;
     std::vector<int> tex_off, tex_w, tex_h;   /* image textures of the committed scene */
+    std::vector<int> mask_cond, mask_marg;    /* masked-aperture distributions per texture (-1: none) */
+    std::vector<float> mask_int;
     int num_media = 0, num_materials = 0;
     bool tuned = false;         /* lgpu_autotune result, used by kernel_mode AUTO */
     lgpu_tuning tuning;
@@ -124,6 +126,8 @@ inline lt::V3f v3(const float *p) { lt::V3f r; r.x = p[0]; r.y = p[1]; r.z = p[2
 struct HostScene {
     DeviceScene S;
     std::vector<int> texOff, texW, texH;   /* image textures in the texel pool */
+    std::vector<int> maskCond, maskMarg;   /* per texture: masked-aperture Piecewise2D offsets in fpool (-1: none) */
+    std::vector<float> maskInt;
     std::vector<DNode> nodes;
     std::vector<DTri> tris;
     std::vector<DInst> insts;
@@ -559,6 +563,38 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
         H.texH.push_back(td.height);
         for (int k = 0; k < td.width * td.height; ++k)
             H.envTex.push_back(make_float4(td.rgba[4 * k], td.rgba[4 * k + 1], td.rgba[4 * k + 2], td.rgba[4 * k + 3]));
+        H.maskCond.push_back(-1); H.maskMarg.push_back(-1); H.maskInt.push_back(0.f);
+        if (td.aperture_mask) {
+            /* MaskedAperture::InitDistribution (Aperture.cpp:38-51): |red| of GetPixelUV at texel
+             * corners (bilinear, Texture.h:71-81), then Piecewise2D (Piecewise.cpp:40-58) */
+            const int w = td.width, h = td.height;
+            std::vector<float> img((size_t)w * h);
+            for (int y = 0; y < h; ++y) {
+                const float vp = (float)y / (float)h;
+                for (int x = 0; x < w; ++x) {
+                    const float up = (float)x / (float)w;
+                    const float fx = std::min((float)(w - 1), std::max(std::min(up, 1.f), 0.f) * (float)w);
+                    const float fy = std::min((float)(h - 1), std::max(std::min(vp, 1.f), 0.f) * (float)h);
+                    const unsigned xi = (unsigned)fx, yi = (unsigned)fy;
+                    const unsigned x1 = std::min(xi + 1, (unsigned)w - 1), y1 = std::min(yi + 1, (unsigned)h - 1);
+                    const float r00 = td.rgba[4 * ((size_t)yi * w + xi)], r10 = td.rgba[4 * ((size_t)yi * w + x1)];
+                    const float r01 = td.rgba[4 * ((size_t)y1 * w + xi)], r11 = td.rgba[4 * ((size_t)y1 * w + x1)];
+                    const float ya = r00 + (r10 - r00) * (fx - (float)xi);
+                    const float yb = r01 + (r11 - r01) * (fx - (float)xi);
+                    img[x + (size_t)y * w] = std::abs(ya + (yb - ya) * (fy - (float)yi));
+                }
+            }
+            std::vector<float> rowInt(h);
+            H.maskCond[t] = (int)H.fpool.size();
+            for (int y = 0; y < h; ++y) {
+                int off;
+                rowInt[y] = lt::piecewise1d(&img[(size_t)y * w], (unsigned)w, H.fpool, off);
+                H.fpool.push_back(rowInt[y]);
+            }
+            int marg;
+            H.maskInt[t] = lt::piecewise1d(rowInt.data(), (unsigned)h, H.fpool, marg);
+            H.maskMarg[t] = marg;
+        }
     }
     GraphCompiler gc;
     gc.d = d;
@@ -824,6 +860,7 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
     if (!ok) { free_scene(c); return c->err.find("alloc") != std::string::npos ? LGPU_ERR_OOM : LGPU_ERR_CUDA; }
     c->S = S;
     c->tex_off = H.texOff; c->tex_w = H.texW; c->tex_h = H.texH;
+    c->mask_cond = H.maskCond; c->mask_marg = H.maskMarg; c->mask_int = H.maskInt;
     c->num_media = (int)H.media.size();
     c->num_materials = (int)H.mats.size();
     c->have_scene = true;
@@ -840,8 +877,9 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
 
 namespace {
 
-CamParams make_cam(const lgpu_camera_desc *cd, const lgpu_render_opts *o) {
+CamParams make_cam(const lgpu_context *c, const lgpu_camera_desc *cd, const lgpu_render_opts *o) {
     CamParams cam;
+    std::memset(&cam, 0, sizeof(cam));
     cam.o = make_float3(cd->origin[0], cd->origin[1], cd->origin[2]);
     cam.x = make_float3(cd->x_hat[0], cd->x_hat[1], cd->x_hat[2]);
     cam.y = make_float3(cd->y_hat[0], cd->y_hat[1], cd->y_hat[2]);
@@ -853,7 +891,40 @@ CamParams make_cam(const lgpu_camera_desc *cd, const lgpu_render_opts *o) {
     cam.yi = 1.f / (float)o->height;
     cam.W = o->width;
     cam.H = o->height;
+    cam.type = cd->type;
+    cam.aperture = cd->type == LGPU_CAMERA_THIN_LENS ? cd->aperture : LGPU_APERTURE_NONE;
+    cam.blades = cd->blades;
+    cam.focal = cd->focal_length;
+    cam.ap_size = cd->aperture_size;
+    cam.off_phi = cd->offset_phi;
+    cam.off_theta = cd->offset_theta;
+    if (cam.aperture == LGPU_APERTURE_MASKED) {   /* index checked by check_camera */
+        const int t = cd->aperture_mask;
+        cam.mask_cond_off = c->mask_cond[t];
+        cam.mask_marg_off = c->mask_marg[t];
+        cam.mask_w = c->tex_w[t];
+        cam.mask_h = c->tex_h[t];
+        cam.mask_marg_int = c->mask_int[t];
+    }
     return cam;
+}
+
+/* Camera parameters a kernel relies on: known type and aperture, a blade count that divides the
+ * circle, a masked aperture's texture committed with its distribution, finite lens values. */
+int check_camera(lgpu_context *c, const lgpu_camera_desc *cd) {
+    if (cd->type < LGPU_CAMERA_PINHOLE || cd->type > LGPU_CAMERA_SPHERICAL) return fail(c, LGPU_ERR_INVALID_ARG, "unknown camera type");
+    if (!std::isfinite(cd->fov) || !std::isfinite(cd->offset_phi) || !std::isfinite(cd->offset_theta))
+        return fail(c, LGPU_ERR_INVALID_ARG, "camera parameters must be finite");
+    if (cd->type != LGPU_CAMERA_THIN_LENS) return LGPU_OK;
+    if (!std::isfinite(cd->focal_length) || !std::isfinite(cd->aperture_size)) return fail(c, LGPU_ERR_INVALID_ARG, "lens parameters must be finite");
+    if (cd->aperture < LGPU_APERTURE_NONE || cd->aperture > LGPU_APERTURE_MASKED) return fail(c, LGPU_ERR_INVALID_ARG, "unknown aperture type");
+    if (cd->aperture == LGPU_APERTURE_BLADE && cd->blades < 1) return fail(c, LGPU_ERR_INVALID_ARG, "a blade aperture needs at least one blade");
+    if (cd->aperture == LGPU_APERTURE_MASKED) {
+        const int t = cd->aperture_mask;
+        if (t < 0 || t >= (int)c->mask_cond.size() || c->mask_cond[t] < 0)
+            return fail(c, LGPU_ERR_INVALID_ARG, "masked aperture: texture not committed with aperture_mask set");
+    }
+    return LGPU_OK;
 }
 
 int check_opts(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_opts *o) {
@@ -865,7 +936,7 @@ int check_opts(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_o
     if (o->integrator < LGPU_INTEGRATOR_PATH || o->integrator > LGPU_INTEGRATOR_GPU_MISVOLPATH ||
         o->integrator == LGPU_INTEGRATOR_AOV)
         return fail(c, LGPU_ERR_INVALID_ARG, "integrator not available on the GPU path (AOV passes are not built)");
-    return LGPU_OK;
+    return check_camera(c, cam);
 }
 
 /* Grow the wavefront pool to `slots` path slots of `state_bytes` each. */
@@ -991,7 +1062,7 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     WaveArgs W;
     std::memset(&W, 0, sizeof(W));
     W.S = c->S;
-    W.cam = make_cam(cam, o);
+    W.cam = make_cam(c, cam, o);
     W.rp.spp = o->spp; W.rp.max_bounces = o->max_bounces; W.rp.min_bounces = o->min_bounces;
     W.rp.seed = o->seed; W.rp.sample_offset = o->sample_offset;
     W.states = c->w_states;
@@ -1189,7 +1260,7 @@ int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_
     }
     LaunchArgs a;
     a.S = c->S;
-    a.cam = make_cam(cam, o);
+    a.cam = make_cam(c, cam, o);
     a.rp.spp = o->spp;
     a.rp.max_bounces = o->max_bounces;
     a.rp.min_bounces = o->min_bounces;
@@ -1374,7 +1445,7 @@ int check_view(lgpu_context *c, const lgpu_view_desc &v) {
     if (v.max_bounces < 0) return fail(c, LGPU_ERR_INVALID_ARG, "negative bounce count in a view");
     if ((uint64_t)v.width * v.height > (1ull << 32) - 1) return fail(c, LGPU_ERR_INVALID_ARG, "view film too large");
     if (!v.film_dev) return fail(c, LGPU_ERR_INVALID_ARG, "null view film");
-    return LGPU_OK;
+    return check_camera(c, &v.camera);
 }
 
 lgpu_render_opts view_opts(const lgpu_render_opts *o, const lgpu_view_desc &v) {
@@ -1391,7 +1462,7 @@ int batch_chunk(lgpu_context *c, const lgpu_view_desc *views, int v0, int v1, co
     for (int v = v0; v < v1; ++v) {
         const lgpu_render_opts vo = view_opts(o, views[v]);
         DView &d = table[(size_t)(v - v0)];
-        d.cam = make_cam(&views[v].camera, &vo);
+        d.cam = make_cam(c, &views[v].camera, &vo);
         d.rp.spp = vo.spp; d.rp.max_bounces = vo.max_bounces; d.rp.min_bounces = vo.min_bounces;
         d.rp.seed = vo.seed; d.rp.sample_offset = vo.sample_offset;
         d.first = total;
@@ -1456,7 +1527,7 @@ LGPU_API int lgpu_render_batch(lgpu_context *c, const lgpu_view_desc *views, int
             const uint64_t n = (uint64_t)vo.width * vo.height * vo.spp;
             LaunchArgs a;
             a.S = c->S;
-            a.cam = make_cam(&views[v].camera, &vo);
+            a.cam = make_cam(c, &views[v].camera, &vo);
             a.rp.spp = vo.spp; a.rp.max_bounces = vo.max_bounces; a.rp.min_bounces = vo.min_bounces;
             a.rp.seed = vo.seed; a.rp.sample_offset = vo.sample_offset; a.rp.integrator = vo.integrator;
             a.film = reinterpret_cast<float4 *>(views[v].film_dev);
@@ -1605,7 +1676,7 @@ LGPU_API int lgpu_adjoint(lgpu_context *c, const lgpu_camera_desc *cam, const lg
     const uint64_t n = (uint64_t)o->width * o->height * o->spp;
     cudaStream_t st = (cudaStream_t)stream;
     cudaEventRecord(c->ev0, st);
-    cudaError_t e = launch_adjoint(c->S, make_cam(cam, o), rp, A, n, st);
+    cudaError_t e = launch_adjoint(c->S, make_cam(c, cam, o), rp, A, n, st);
     if (e != cudaSuccess) return cuda_fail(c, e, "adjoint launch");
     cudaEventRecord(c->ev1, st);
     c->stats.paths = n;
@@ -1699,7 +1770,7 @@ LGPU_API int lgpu_render_paths_noalloc(lgpu_context *c, const lgpu_camera_desc *
     WaveArgs W;
     std::memset(&W, 0, sizeof(W));
     W.S = c->S;
-    W.cam = make_cam(cam, o);
+    W.cam = make_cam(c, cam, o);
     W.rp.spp = o->spp; W.rp.max_bounces = o->max_bounces; W.rp.min_bounces = o->min_bounces;
     W.rp.seed = o->seed; W.rp.sample_offset = o->sample_offset;
     W.states = base;

@@ -11,6 +11,14 @@ struct CamParams {
     float tanFov, tanFov2, aspect;
     float xi, yi;   /* 1 / width, 1 / height */
     int W, H;
+    int type;       /* lgpu_camera_type */
+    int aperture;   /* lgpu_aperture_type (thin lens) */
+    int blades;
+    float focal, ap_size, off_phi, off_theta;
+    /* masked aperture: Piecewise2D of the mask in the scene's float pool (rows of 2w + 2 floats:
+     * CDF, function, integral; then the marginal CDF and function) */
+    int mask_cond_off, mask_marg_off, mask_w, mask_h;
+    float mask_marg_int;
 };
 struct RenderParams {
     int spp, max_bounces, min_bounces;

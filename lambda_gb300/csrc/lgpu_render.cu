@@ -11,6 +11,7 @@
 
 #include <algorithm>
 
+#include "lgpu_camera.cuh"
 #include "lgpu_integrator.cuh"
 #include "lgpu_launch.h"
 #include "lgpu_wavefront.cuh"
@@ -68,21 +69,18 @@ __global__ void __launch_bounds__(128) k_render(const __grid_constant__ DeviceSc
                 lam.l[k] = l;
             }
         }
-        /* pixel jitter (Render.cpp:55-56) and PinholeCamera::GenerateRay (Camera.cpp:41-44) */
-        const float u = cam.xi * ((float)x + rng.next() - .5f);
-        const float v = cam.yi * ((float)y + rng.next() - .5f);
-        const float3 p = cam.o + cam.x * (u * -cam.tanFov2 + cam.tanFov) +
-                         cam.y * (v * -cam.tanFov2 * cam.aspect + cam.tanFov * cam.aspect) + cam.z;
-        const float3 d = normalised(p - cam.o);
+        /* pixel jitter (Render.cpp:55-56) and Camera::GenerateRay (Camera.cpp:41-71) */
+        float3 o, d;
+        camera_ray(cam, S.fpool, x, y, rng, o, d);
         Tracer<NS, COUNT> T{S, rng, lam, &st};
         Spec<NS> L;
         switch (rp.integrator) {
-        case LGPU_INTEGRATOR_PATH: L = T.Li_path(cam.o, d, rp.max_bounces, rp.min_bounces); break;
-        case LGPU_INTEGRATOR_VOLPATH: L = T.Li_volpath(cam.o, d, rp.max_bounces, rp.min_bounces); break;
-        case LGPU_INTEGRATOR_DIRECT: L = T.Li_direct(cam.o, d); break;
-        case LGPU_INTEGRATOR_NORMAL: L = T.Li_pass(cam.o, d, true); break;
-        case LGPU_INTEGRATOR_DEPTH: L = T.Li_pass(cam.o, d, false); break;
-        default: L = T.Li(cam.o, d, rp.max_bounces, rp.min_bounces); break;
+        case LGPU_INTEGRATOR_PATH: L = T.Li_path(o, d, rp.max_bounces, rp.min_bounces); break;
+        case LGPU_INTEGRATOR_VOLPATH: L = T.Li_volpath(o, d, rp.max_bounces, rp.min_bounces); break;
+        case LGPU_INTEGRATOR_DIRECT: L = T.Li_direct(o, d); break;
+        case LGPU_INTEGRATOR_NORMAL: L = T.Li_pass(o, d, true); break;
+        case LGPU_INTEGRATOR_DEPTH: L = T.Li_pass(o, d, false); break;
+        default: L = T.Li(o, d, rp.max_bounces, rp.min_bounces); break;
         }
         hero_to_rgb<NS>(L, lam, rgb);
         /* w = random numbers drawn: a control-flow fingerprint of the path */
@@ -141,16 +139,13 @@ __global__ void __launch_bounds__(128) k_adjoint(const __grid_constant__ DeviceS
         rng.key = lgpu_path_key(rp.seed, pixel, sidx);
         rng.dim = 0;
         Lambda4 lam;
-        const float u = cam.xi * ((float)x + rng.next() - .5f);
-        const float v = cam.yi * ((float)y + rng.next() - .5f);
-        const float3 p = cam.o + cam.x * (u * -cam.tanFov2 + cam.tanFov) +
-                         cam.y * (v * -cam.tanFov2 * cam.aspect + cam.tanFov * cam.aspect) + cam.z;
-        const float3 d = normalised(p - cam.o);
+        float3 o, d;
+        camera_ray(cam, S.fpool, x, y, rng, o, d);
         const float4 dd = A.dloss[pixel];
         const float3 dl = make_float3(dd.x * A.inv_spp, dd.y * A.inv_spp, dd.z * A.inv_spp);
         TravStats st = {0u, 0u, 0u};
         Tracer<3, false> T{S, rng, lam, &st};
-        T.Li_adj(cam.o, d, rp.max_bounces, rp.min_bounces, A, dl, g);
+        T.Li_adj(o, d, rp.max_bounces, rp.min_bounces, A, dl, g);
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {

@@ -15,6 +15,7 @@
  */
 #pragma once
 #include <cooperative_groups.h>
+#include "lgpu_camera.cuh"
 #include "lgpu_integrator.cuh"
 #include "lgpu_launch.h"
 
@@ -345,7 +346,7 @@ struct Wave {
         W.path_out[s.out] = make_float4(rgb[0], rgb[1], rgb[2], (float)rng.dim);
     }
 
-    /* Start path number `idx` of the chunk in this slot (camera ray, Render.cpp:55-56 + Camera.cpp:41-44). */
+    /* Start path number `idx` of the chunk in this slot (camera ray, Render.cpp:55-56 + Camera.cpp:41-71). */
     __device__ void start_path(uint64_t idx) {
         int view = 0;
         uint64_t pid;
@@ -381,12 +382,7 @@ struct Wave {
                 lam.l[k] = l;
             }
         }
-        const float u = cam.xi * ((float)x + rng.next() - .5f);
-        const float v = cam.yi * ((float)y + rng.next() - .5f);
-        const float3 p = cam.o + cam.x * (u * -cam.tanFov2 + cam.tanFov) +
-                         cam.y * (v * -cam.tanFov2 * cam.aspect + cam.tanFov * cam.aspect) + cam.z;
-        s.ro = cam.o;
-        s.rd = normalised(p - cam.o);
+        camera_ray(cam, W.S.fpool, x, y, rng, s.ro, s.rd);
         s.L = Spec<NS>(0.f);
         s.beta = Spec<NS>(1.f);
         s.hit.tFar = finf(); s.hit.uv = make_float2(0.f, 0.f);

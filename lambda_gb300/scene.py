@@ -15,10 +15,20 @@ def _fptr(a):
 
 
 class Camera:
-    """Pinhole camera with the axes convention of Camera::SetForwards (src/camera/Camera.cpp:28-32):
-    z = forward, x = cross(z, up), y = cross(x, z)."""
+    """Camera with the axes convention of Camera::SetForwards (src/camera/Camera.cpp:28-32):
+    z = forward, x = cross(z, up), y = cross(x, z).
 
-    def __init__(self, origin, target, fov=1.1, up=(0.0, 1.0, 0.0)):
+    kind: "pinhole" (PinholeCamera), "thin_lens" (ThinLensCamera: focal_length, aperture "none",
+    "circular", "blade" or "masked" with aperture_size, blades and aperture_mask = index of a texture
+    added with aperture_mask=True) or "spherical" (SphericalCamera: offset_phi, offset_theta)."""
+
+    KINDS = {"pinhole": abi.CAMERA_PINHOLE, "thin_lens": abi.CAMERA_THIN_LENS, "spherical": abi.CAMERA_SPHERICAL}
+    APERTURES = {"none": abi.APERTURE_NONE, "circular": abi.APERTURE_CIRCULAR, "blade": abi.APERTURE_BLADE,
+                 "masked": abi.APERTURE_MASKED}
+
+    def __init__(self, origin, target, fov=1.1, up=(0.0, 1.0, 0.0), kind="pinhole", focal_length=1.0,
+                 aperture="none", aperture_size=0.0, blades=6, aperture_mask=-1, offset_phi=0.0,
+                 offset_theta=0.0):
         o = np.asarray(origin, np.float64)
         z = np.asarray(target, np.float64) - o
         z /= np.linalg.norm(z)
@@ -26,13 +36,22 @@ class Camera:
         x /= np.linalg.norm(x)
         y = np.cross(x, z)
         self.origin, self.x, self.y, self.z, self.fov = o, x, y, z, float(fov)
+        self.kind, self.focal_length, self.aperture = kind, float(focal_length), aperture
+        self.aperture_size, self.blades, self.aperture_mask = float(aperture_size), int(blades), int(aperture_mask)
+        self.offset_phi, self.offset_theta = float(offset_phi), float(offset_theta)
 
     def desc(self):
         d = abi.CameraDesc()
         for name, v in (("origin", self.origin), ("x_hat", self.x), ("y_hat", self.y), ("z_hat", self.z)):
             getattr(d, name)[:] = [float(t) for t in v]
         d.fov = self.fov
-        d.type = 0
+        d.type = self.KINDS[self.kind]
+        d.focal_length = self.focal_length
+        d.aperture = self.APERTURES[self.aperture]
+        d.aperture_size = self.aperture_size
+        d.blades = self.blades
+        d.aperture_mask = self.aperture_mask
+        d.offset_phi, d.offset_theta = self.offset_phi, self.offset_theta
         return d
 
 
@@ -41,6 +60,7 @@ class SceneBuilder:
         self.meshes, self.objects, self.materials = [], [], []
         self.nodes, self.lights, self.media = [], [], []
         self.textures = []
+        self.texture_masks = []
         self.has_volumes = False
         self.light_strategy = abi.LIGHT_STRATEGY_TREE
         self._keep = []
@@ -136,14 +156,16 @@ class SceneBuilder:
         self.media.append((sa, ss, g))
         return len(self.media) - 1
 
-    def texture(self, rgba):
+    def texture(self, rgba, aperture_mask=False):
         """Image texture (height, width, 4) float texels, row y then column x; returns its index
-        for an IMAGE_TEXTURE node's params[0]."""
+        for an IMAGE_TEXTURE node's params[0] or a masked aperture (aperture_mask=True builds the
+        sampling distribution of its |red| channel at commit)."""
         t = np.ascontiguousarray(rgba, np.float32)
         if t.ndim == 3 and t.shape[2] == 3:
             t = np.ascontiguousarray(np.concatenate([t, np.ones(t.shape[:2] + (1,), np.float32)], 2))
         assert t.ndim == 3 and t.shape[2] == 4
         self.textures.append(t)
+        self.texture_masks.append(bool(aperture_mask))
         return len(self.textures) - 1
 
     # ---------------------------------------------------------------- descriptor
@@ -170,6 +192,7 @@ class SceneBuilder:
         texs = (abi.TextureDesc * max(1, len(self.textures)))()
         for i, t in enumerate(self.textures):
             texs[i].rgba, texs[i].height, texs[i].width = _fptr(t), t.shape[0], t.shape[1]
+            texs[i].aperture_mask = int(self.texture_masks[i])
         d = abi.SceneDesc(ms, len(self.meshes), obs, len(self.objects), mats, len(self.materials),
                           nodes, len(self.nodes), lights, len(self.lights), media, len(self.media),
                           int(self.has_volumes), int(self.light_strategy), texs, len(self.textures))

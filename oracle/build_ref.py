@@ -1,4 +1,4 @@
-"""Build oracle/_ref/libref_kat.so: the golden-vector driver (oracle/ref_kat.cpp) linked with six of
+"""Build oracle/_ref/libref_kat.so: the golden-vector driver (oracle/ref_kat.cpp) linked with nine of
 the reference renderer's translation units, compiled with g++ from the reference tree where it lies.
 TEST INFRASTRUCTURE ONLY; the output stays in oracle/_ref/ and never ships.
 
@@ -17,7 +17,11 @@ HERE = pathlib.Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 LIB = OUT / "libref_kat.so"
 UNITS = ["shading/Fresnel.cpp", "shading/media/HenyeyGreenstein.cpp", "shading/media/HomogeneousMedium.cpp",
-         "core/Spectrum.cpp", "core/SPD_Data.cpp", "sampling/Piecewise.cpp"]
+         "core/Spectrum.cpp", "core/SPD_Data.cpp", "sampling/Piecewise.cpp", "camera/Camera.cpp", "camera/Aperture.cpp",
+         "image/TextureEncoding.cpp"]
+# camera/Aperture.cpp instantiates the reference's texture class, whose Morton-order addressing calls the
+# x86 BMI2 intrinsic _pdep_u64 (image/Texture.h:46): that unit needs -mbmi2 (this x86 build only).
+UNIT_FLAGS = {"camera/Aperture.cpp": ["-mbmi2"]}
 
 
 def build(ref_root="/root/reference", force=False):
@@ -32,7 +36,7 @@ def build(ref_root="/root/reference", force=False):
     objs = []
     for u in UNITS:
         obj = OUT / (u.replace("/", "_") + ".o")
-        subprocess.run(flags + ["-c", str(src / u), "-o", str(obj)], check=True)
+        subprocess.run(flags + UNIT_FLAGS.get(u, []) + ["-c", str(src / u), "-o", str(obj)], check=True)
         objs.append(str(obj))
     drv = OUT / "ref_kat.o"
     subprocess.run(flags + ["-c", str(HERE / "ref_kat.cpp"), "-o", str(drv)], check=True)

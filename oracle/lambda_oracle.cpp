@@ -2368,6 +2368,7 @@ struct Integrator {
 /* ------------------------------------------------------------------ scene setup */
 struct Oracle {
     Scene sc;
+    std::vector<std::unique_ptr<Piecewise2D>> masks;   /* per texture: masked-aperture distribution or null */
     std::string err;
     bool Load(const lgpu_scene_desc *d);
 };
@@ -2394,6 +2395,28 @@ bool Oracle::Load(const lgpu_scene_desc *d) {
         sc.graph.tex.emplace_back(td.rgba, td.rgba + (size_t)td.width * td.height * 4);
         sc.graph.texW.push_back(td.width);
         sc.graph.texH.push_back(td.height);
+        masks.emplace_back();
+        if (td.aperture_mask) {
+            /* MaskedAperture::InitDistribution (Aperture.cpp:38-51): |GetPixelUV(x/w, y/h).r|,
+             * bilinear (Texture.h:71-81) */
+            const int w = td.width, h = td.height;
+            std::vector<Real> img((size_t)w * h);
+            for (int y = 0; y < h; ++y) {
+                const float vp = (float)y / (float)h;
+                for (int x = 0; x < w; ++x) {
+                    const float up = (float)x / (float)w;
+                    const float fx = std::min((float)(w - 1), clampr(up, 0.f, 1.f) * (float)w);
+                    const float fy = std::min((float)(h - 1), clampr(vp, 0.f, 1.f) * (float)h);
+                    const unsigned xi = (unsigned)fx, yi = (unsigned)fy;
+                    const unsigned x1 = std::min(xi + 1, (unsigned)w - 1), y1 = std::min(yi + 1, (unsigned)h - 1);
+                    auto R = [&](unsigned xx, unsigned yy) { return td.rgba[4 * ((size_t)yy * w + xx)]; };
+                    const float ya = Lerp(R(xi, yi), R(x1, yi), fx - (float)xi);
+                    const float yb = Lerp(R(xi, y1), R(x1, y1), fx - (float)xi);
+                    img[x + (size_t)y * w] = std::abs(Lerp(ya, yb, fy - (float)yi));
+                }
+            }
+            masks.back().reset(new Piecewise2D(img.data(), (unsigned)w, (unsigned)h));
+        }
     }
     sc.hasVolumes = d->has_volumes != 0;
     sc.meshes.resize(d->num_meshes);
@@ -2526,7 +2549,60 @@ static void SetWavelengths(uint32_t key) {
     }
 }
 
-/* One path: pixel jitter (Render.cpp:55-56), pinhole ray (Camera.cpp:41-44), Li. */
+/* Aperture::Sample_p (Aperture.cpp:10-36) */
+static V2 ApertureSample(const Oracle *o, const lgpu_camera_desc &c, Sampler &s) {
+    const Real size = c.aperture_size;
+    switch (c.aperture) {
+    case LGPU_APERTURE_BLADE: {   /* BladeAperture::Sample_p (Aperture.cpp:10-19) */
+        const Real d = PI2 / (Real)c.blades;
+        const Real rnd = PI2 * s.Get1D();
+        const Real thetaMin = std::floor(rnd / d) * d;
+        const Real thetaMax = thetaMin + d;
+        const V2 p1(std::cos(thetaMin), std::sin(thetaMin)), p2(std::cos(thetaMax), std::sin(thetaMax));
+        const Real ux = s.Get1D(), uy = s.Get1D();
+        return V2((p1.x * ux + p2.x * uy) * size, (p1.y * ux + p2.y * uy) * size);
+    }
+    case LGPU_APERTURE_CIRCULAR: {   /* CircularAperture::Sample_p (Aperture.cpp:25-27) + SampleUnitDisk */
+        const Real ux = s.Get1D(), uy = s.Get1D();
+        const Real r = std::sqrt(ux), theta = uy * PI2;
+        return V2(r * std::cos(theta) * size - size * (Real).5, r * std::sin(theta) * size - size * (Real).5);
+    }
+    case LGPU_APERTURE_MASKED: {   /* MaskedAperture::Sample_p (Aperture.cpp:33-36) */
+        const Real ux = s.Get1D(), uy = s.Get1D();
+        Real pdf;
+        const V2 p = o->masks[c.aperture_mask]->SampleContinuous(V2(ux, uy), &pdf);
+        return V2(p.x * size - size * (Real).5, p.y * size - size * (Real).5);
+    }
+    default: return V2(0, 0);
+    }
+}
+
+/* Camera::GenerateRay (Camera.cpp:41-71) at film coordinates (u, v) of a W x H film; the thin lens
+ * draws its aperture point from s. */
+static Ray GenerateCameraRay(const Oracle *o, const lgpu_camera_desc &c, int W, int H, Real u, Real v, Sampler &s) {
+    const V3 org(c.origin[0], c.origin[1], c.origin[2]);
+    const V3 xh(c.x_hat[0], c.x_hat[1], c.x_hat[2]), yh(c.y_hat[0], c.y_hat[1], c.y_hat[2]), zh(c.z_hat[0], c.z_hat[1], c.z_hat[2]);
+    const Real tanFov = (Real)std::tan(.5 * c.fov);
+    const Real tanFov2 = 2 * tanFov;
+    const Real aspect = (Real)H / (Real)W;
+    if (c.type == LGPU_CAMERA_SPHERICAL) {   /* SphericalCamera::GenerateRay (Camera.cpp:66-71) */
+        const Real phi = PI2 * u + c.offset_phi;
+        const Real theta = PI * v + c.offset_theta;
+        const V3 d = SphericalDirection(std::sin(theta), std::cos(theta), phi).Normalised();
+        return Ray{org, xh * d.x + yh * d.y + zh * d.z};
+    }
+    if (c.type == LGPU_CAMERA_THIN_LENS) {   /* ThinLensCamera::GenerateRay (Camera.cpp:53-58) */
+        const V3 fp = org + (xh * (u * -tanFov2 + tanFov) + yh * (v * -tanFov2 * aspect + tanFov * aspect) + zh) * (Real)c.focal_length;
+        const V2 ap = c.aperture != LGPU_APERTURE_NONE ? ApertureSample(o, c, s) : V2(0, 0);
+        const V3 ro = org + xh * ap.x + yh * ap.y;
+        return Ray{ro, (fp - ro).Normalised()};
+    }
+    /* PinholeCamera::GenerateRay (Camera.cpp:41-44) */
+    const V3 p = org + xh * (u * -tanFov2 + tanFov) + yh * (v * -tanFov2 * aspect + tanFov * aspect) + zh;
+    return Ray{org, (p - org).Normalised()};
+}
+
+/* One path: pixel jitter (Render.cpp:55-56), Camera::GenerateRay, Li. */
 static Spec TracePath(const OracleRun &R, uint64_t pathId, Real rgbOut[3], uint32_t *dimsOut) {
     const int W = R.opt->width, H = R.opt->height, spp = R.opt->spp;
     const uint32_t pixel = (uint32_t)(pathId / (uint64_t)spp);
@@ -2539,14 +2615,7 @@ static Spec TracePath(const OracleRun &R, uint64_t pathId, Real rgbOut[3], uint3
     const Real xi = (Real)1 / W, yi = (Real)1 / H;
     const Real u = xi * ((Real)x + s.Get1D() - (Real).5);
     const Real v = yi * ((Real)y + s.Get1D() - (Real).5);
-    const lgpu_camera_desc &c = *R.cam;
-    const V3 org(c.origin[0], c.origin[1], c.origin[2]);
-    const V3 xh(c.x_hat[0], c.x_hat[1], c.x_hat[2]), yh(c.y_hat[0], c.y_hat[1], c.y_hat[2]), zh(c.z_hat[0], c.z_hat[1], c.z_hat[2]);
-    const Real tanFov = (Real)std::tan(.5 * c.fov);
-    const Real tanFov2 = 2 * tanFov;
-    const Real aspect = (Real)H / (Real)W;
-    const V3 p = org + xh * (u * -tanFov2 + tanFov) + yh * (v * -tanFov2 * aspect + tanFov * aspect) + zh;
-    Ray r{org, (p - org).Normalised()};
+    const Ray r = GenerateCameraRay(R.o, *R.cam, W, H, u, v, s);
     Integrator I(R.o->sc, R.opt->max_bounces, R.opt->min_bounces);
     Spec L;
     switch (R.opt->integrator) {
@@ -2656,6 +2725,30 @@ LGPU_API void oracle_microfacet(int dist, const float *wh, const float *wo, cons
     out[3] = DistPdf(dist, h, V2(ax, ay));
 }
 LGPU_API float oracle_to_alpha(float r) { return ToAlpha(r); }
+/* Same arguments as the reference-side driver's camera entry point: type 0 pinhole, 1 thin lens,
+ * 2 spherical; aperture 0 none, 1 circular, 2 blade (known-answer tests) */
+LGPU_API void oracle_kat_camera_ray(int type, const float *org, const float *xh, const float *yh, const float *zh, float fov,
+                                    int W, int H, float focal, int aperture, float size, int blades, float offPhi,
+                                    float offTheta, float u, float v, const float *ap_u, float *o, float *d) {
+    lgpu_camera_desc c;
+    std::memset(&c, 0, sizeof(c));
+    for (int k = 0; k < 3; ++k) { c.origin[k] = org[k]; c.x_hat[k] = xh[k]; c.y_hat[k] = yh[k]; c.z_hat[k] = zh[k]; }
+    c.fov = fov; c.type = type; c.focal_length = focal; c.aperture = aperture; c.aperture_size = size;
+    c.blades = blades; c.offset_phi = offPhi; c.offset_theta = offTheta;
+    Sampler s; s.replay = ap_u;
+    const Ray r = GenerateCameraRay(nullptr, c, W, H, u, v, s);
+    o[0] = r.o.x; o[1] = r.o.y; o[2] = r.o.z;
+    d[0] = r.d.x; d[1] = r.d.y; d[2] = r.d.z;
+}
+/* Camera::GenerateRay at film coordinates (u, v) with the aperture's numbers replayed from ap_u
+ * (known-answer tests; handle may be null unless the aperture is masked) */
+LGPU_API void oracle_camera_ray(void *handle, const lgpu_camera_desc *cam, int W, int H, float u, float v,
+                                const float *ap_u, float *o, float *d) {
+    Sampler s; s.replay = ap_u;
+    const Ray r = GenerateCameraRay((const Oracle *)handle, *cam, W, H, u, v, s);
+    o[0] = r.o.x; o[1] = r.o.y; o[2] = r.o.z;
+    d[0] = r.d.x; d[1] = r.d.y; d[2] = r.d.z;
+}
 LGPU_API float oracle_phase_hg(float c, float g) { return Medium::PhaseHG(c, g); }
 /* HG Sample_p with explicit u: returns pdf, writes wi */
 LGPU_API float oracle_hg_sample(float g, const float *wo, float u0, float u1, float *wi) {

@@ -2,11 +2,12 @@
  * ref_kat.cpp -- golden-vector driver over the reference renderer's OWN translation units.
  * TEST INFRASTRUCTURE ONLY: built by oracle/build_ref.py into oracle/_ref/ together with the
  * reference's Fresnel.cpp, HenyeyGreenstein.cpp, HomogeneousMedium.cpp, Spectrum.cpp,
- * SPD_Data.cpp and Piecewise.cpp compiled where they lie; used to pin the oracle's restatement of
- * those functions (tests/golden).  Each entry point calls the reference function named beside it
+ * SPD_Data.cpp, Piecewise.cpp, Camera.cpp, Aperture.cpp and TextureEncoding.cpp compiled where they
+ * lie; used to pin the oracle's restatement of those functions (tests/golden).  Each entry point calls the reference function named beside it
  * with fixed inputs; random numbers come from a sampler that replays given values.
  */
 #include <Lambda.h>
+#include <camera/Camera.h>
 #include <core/Ray.h>
 #include <core/Spectrum.h>
 #include <sampling/Piecewise.h>
@@ -126,4 +127,29 @@ REF_API void ref_piecewise2d(const float *f, int nu, int nv, float u0, float u1,
     Real pdf = 0;
     const Vec2 x = d.SampleContinuous(Vec2(u0, u1), &pdf);
     out[0] = x.x; out[1] = x.y; out[2] = pdf; out[3] = d.PDF(x);
+}
+
+/* PinholeCamera / ThinLensCamera / SphericalCamera::GenerateRay (camera/Camera.cpp:41-71) with a
+ * CircularAperture or BladeAperture (camera/Aperture.cpp:10-27) drawing from ap_u.
+ * type 0 pinhole, 1 thin lens, 2 spherical; aperture 0 none, 1 circular, 2 blade. */
+REF_API void ref_camera_ray(int type, const float *org, const float *xh, const float *yh, const float *zh, float fov,
+                            int W, int H, float focal, int aperture, float size, int blades, float offPhi,
+                            float offTheta, float u, float v, const float *ap_u, float *o, float *d) {
+    ReplaySampler s(ap_u, 8);
+    const Vec3 origin(org[0], org[1], org[2]);
+    std::unique_ptr<Aperture> ap;
+    if (aperture == 1) ap.reset(new CircularAperture(size));
+    if (aperture == 2) ap.reset(new BladeAperture((unsigned)blades, size));
+    std::unique_ptr<Camera> cam;
+    if (type == 1) cam.reset(new ThinLensCamera(origin, (Real)W, (Real)H, focal, ap.get()));
+    else if (type == 2) {
+        SphericalCamera *sc = new SphericalCamera(origin);
+        sc->offsetPhi = offPhi;
+        sc->offsetTheta = offTheta;
+        cam.reset(sc);
+    } else cam.reset(new PinholeCamera(origin, (Real)W, (Real)H));
+    cam->SetAxes(Vec3(xh[0], xh[1], xh[2]), Vec3(yh[0], yh[1], yh[2]), Vec3(zh[0], zh[1], zh[2]));
+    cam->SetFov(fov);
+    const Ray r = cam->GenerateRay(u, v, s);
+    for (int k = 0; k < 3; ++k) { o[k] = r.o[k]; d[k] = r.d[k]; }
 }

@@ -1,8 +1,8 @@
 """Generate tests/golden/ref_kat.npz: golden vectors computed by the reference renderer's own code.
 
 Loads oracle/_ref/libref_kat.so (built by oracle/build_ref.py from the reference's Fresnel.cpp,
-HenyeyGreenstein.cpp, HomogeneousMedium.cpp, Spectrum.cpp, SPD_Data.cpp and Piecewise.cpp) and
-evaluates it on seeded inputs.  Needs the reference tree, so it runs where that exists:
+HenyeyGreenstein.cpp, HomogeneousMedium.cpp, Spectrum.cpp, SPD_Data.cpp, Piecewise.cpp, Camera.cpp,
+Aperture.cpp and TextureEncoding.cpp) and evaluates it on seeded inputs.  Needs the reference tree, so it runs where that exists:
 
     python tests/golden/gen_golden.py [reference_root]
 """
@@ -65,6 +65,21 @@ def inputs(seed=7):
     d["pw1_u"] = np.concatenate([rng.uniform(0, 1, 30), [0.0, 0.5, 0.9999999]]).astype(F)
     d["pw2_f"] = [rng.uniform(0, 1, (4, 8)).astype(F), rng.uniform(0, 1, (16, 16)).astype(F) ** 4]
     d["pw2_u"] = rng.uniform(0, 1, (30, 2)).astype(F)
+    # cameras: (type, aperture) pairs, each with random axes, fov, film size and lens values
+    kinds = [(0, 0), (1, 0), (1, 1), (1, 2), (2, 0)] * 12
+    d["cam_kind"] = np.array(kinds, np.int32)
+    n = len(kinds)
+    z = unit(rng, n)
+    x = np.cross(z, np.array([0, 1, 0], F))
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    d["cam_axes"] = np.stack([x, np.cross(x, z), z], 1).astype(F)            # (n, 3, 3): x, y, z
+    d["cam_org"] = rng.uniform(-5, 5, (n, 3)).astype(F)
+    d["cam_fov"] = rng.uniform(0.3, 1.6, n).astype(F)
+    d["cam_wh"] = rng.choice([64, 256, 1920, 1080], (n, 2)).astype(np.int32)
+    d["cam_lens"] = np.stack([rng.uniform(0.5, 8, n), rng.uniform(0, 0.3, n), rng.randint(3, 9, n),
+                              rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)], 1).astype(F)  # focal, size, blades, offPhi, offTheta
+    d["cam_uv"] = rng.uniform(0, 1, (n, 2)).astype(F)
+    d["cam_ap_u"] = rng.uniform(0, 1, (n, 8)).astype(F)
     return d
 
 
@@ -81,7 +96,10 @@ def evaluate(L, prefix, d):
                        ("xyz_to_rgb", [C.c_void_p, C.c_void_p], None),
                        ("rgb_y", [C.c_void_p], C.c_float),
                        ("piecewise1d", [C.c_void_p, C.c_int, C.c_float, C.c_void_p], None),
-                       ("piecewise2d", [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p], None)]:
+                       ("piecewise2d", [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p], None),
+                       ("camera_ray", [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int,
+                                       C.c_int, C.c_float, C.c_int, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float,
+                                       C.c_float, C.c_void_p, C.c_void_p, C.c_void_p], None)]:
         f(n_).argtypes, f(n_).restype = at, rt
     o = {}
     o["fr"] = np.array([f("fr_dielectric")(*r) for r in d["fr_in"]], F)
@@ -129,6 +147,17 @@ def evaluate(L, prefix, d):
             f("piecewise2d")(_p(fc), fn.shape[1], fn.shape[0], u[0], u[1], _p(out))
             res.append(out)
         o["pw2_%d" % j] = np.array(res, F)
+    res = []
+    for i, (t, a) in enumerate(d["cam_kind"]):
+        ax = np.ascontiguousarray(d["cam_axes"][i])
+        org, dd = np.zeros(3, F), np.zeros(3, F)
+        fl, size, blades, ophi, oth = d["cam_lens"][i]
+        f("camera_ray")(int(t), _p(np.ascontiguousarray(d["cam_org"][i])), _p(ax[0]), _p(ax[1]), _p(ax[2]),
+                        float(d["cam_fov"][i]), int(d["cam_wh"][i][0]), int(d["cam_wh"][i][1]), float(fl), int(a),
+                        float(size), int(blades), float(ophi), float(oth), float(d["cam_uv"][i][0]),
+                        float(d["cam_uv"][i][1]), _p(np.ascontiguousarray(d["cam_ap_u"][i])), _p(org), _p(dd))
+        res.append(np.concatenate([org, dd]))
+    o["cam"] = np.array(res, F)
     return o
 
 

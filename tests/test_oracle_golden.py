@@ -1,6 +1,6 @@
 """The oracle's restatement against golden vectors computed by the reference renderer's own code
 (tests/golden/ref_kat.npz, made by tests/golden/gen_golden.py from the reference's Fresnel,
-Henyey-Greenstein, homogeneous-medium, spectrum and piecewise-distribution units).
+Henyey-Greenstein, homogeneous-medium, spectrum, piecewise-distribution, camera and aperture units).
 
 Tolerance: 2e-6 relative (1e-7 absolute) -- both sides are the same float arithmetic built with
 -ffp-contract=off; the slack covers libm differences between hosts.  Indices are exact.
@@ -77,6 +77,16 @@ def test_piecewise(oracle_out, gold):
               gold[k][:, [0, 1, 4, 5, 6]] if k.startswith("pw1") else gold[k])
         if k.startswith("pw1"):
             np.testing.assert_array_equal(o[k][:, [2, 3]], gold[k][:, [2, 3]])
+
+
+def test_cameras(oracle_out, gold):
+    """Pinhole, thin lens (no aperture, circular, blade) and spherical rays: origin and direction."""
+    d, o, _ = oracle_out
+    assert gold["cam"].shape == (len(d["cam_kind"]), 6)
+    close(o["cam"], gold["cam"], rt=2e-6, at=2e-6)
+    # the thin lens with an aperture moves the origin off the camera position
+    moved = (d["cam_kind"][:, 0] == 1) & (d["cam_kind"][:, 1] > 0) & (d["cam_lens"][:, 1] > 0.01)
+    assert np.all(np.linalg.norm(gold["cam"][moved, :3] - d["cam_org"][moved], axis=1) > 1e-4)
 
 
 def _smits_tables():
