@@ -39,7 +39,7 @@ def build(ref_root="/root/reference", force=False):
         subprocess.run(flags + UNIT_FLAGS.get(u, []) + ["-c", str(src / u), "-o", str(obj)], check=True)
         objs.append(str(obj))
     drv = OUT / "ref_kat.o"
-    subprocess.run(flags + ["-c", str(HERE / "ref_kat.cpp"), "-o", str(drv)], check=True)
+    subprocess.run(flags + ["-mbmi2", "-c", str(HERE / "ref_kat.cpp"), "-o", str(drv)], check=True)   # drives texture_t too
     subprocess.run(["g++", "-shared", "-o", str(LIB), str(drv), *objs, "-Wl,--no-undefined"], check=True)
     return LIB
 

@@ -373,6 +373,18 @@ struct Val {
     Spec s;
     int bxdf = -1;
 };
+/* texture_t::GetPixelUVBilinear (Texture.h:71-81) over RGBA texels in scanline rows */
+static void TexBilinear(const float *t, int w, int h, Real u, Real v, Real out[4]) {
+    const Real fx = std::min((float)(w - 1), clampr(u, 0.f, 1.f) * (float)w);
+    const Real fy = std::min((float)(h - 1), clampr(v, 0.f, 1.f) * (float)h);
+    const unsigned x = (unsigned)fx, y = (unsigned)fy;
+    const unsigned x1 = std::min(x + 1, (unsigned)w - 1), y1 = std::min(y + 1, (unsigned)h - 1);
+    for (int k = 0; k < 4; ++k) {
+        const Real ya = Lerp(t[4 * ((size_t)y * w + x) + k], t[4 * ((size_t)y * w + x1) + k], fx - (float)x);
+        const Real yb = Lerp(t[4 * ((size_t)y1 * w + x) + k], t[4 * ((size_t)y1 * w + x1) + k], fx - (float)x);
+        out[k] = Lerp(ya, yb, fy - (float)y);
+    }
+}
 struct Graph;
 static Val EvalOutput(const Graph &g, int node, int out, const ScatterEvent &ev);
 
@@ -602,17 +614,7 @@ static Val EvalOutput(const Graph &g, int node, int out, const ScatterEvent &ev)
         const int ti = (int)d.params[0];
         const std::vector<float> &t = g.tex[ti];
         const int w = g.texW[ti], h = g.texH[ti];
-        const V2 uv(Fract(ev.hit->uv.x), Fract(ev.hit->uv.y));
-        /* texture_t::GetPixelUVBilinear (Texture.h:71-81) */
-        const Real fx = std::min((float)(w - 1), clampr(uv.x, 0.f, 1.f) * (float)w);
-        const Real fy = std::min((float)(h - 1), clampr(uv.y, 0.f, 1.f) * (float)h);
-        const unsigned x = (unsigned)fx, y = (unsigned)fy;
-        const unsigned x1 = std::min(x + 1, (unsigned)w - 1), y1 = std::min(y + 1, (unsigned)h - 1);
-        for (int k = 0; k < 4; ++k) {
-            const Real ya = Lerp(t[4 * ((size_t)y * w + x) + k], t[4 * ((size_t)y * w + x1) + k], fx - (float)x);
-            const Real yb = Lerp(t[4 * ((size_t)y1 * w + x) + k], t[4 * ((size_t)y1 * w + x1) + k], fx - (float)x);
-            r.v[k] = Lerp(ya, yb, fy - (float)y);
-        }
+        TexBilinear(t.data(), w, h, Fract(ev.hit->uv.x), Fract(ev.hit->uv.y), r.v);
         if (out == 1) { r.v[1] = r.v[2] = r.v[3] = 0; }
         break;
     }
@@ -2725,6 +2727,17 @@ LGPU_API void oracle_microfacet(int dist, const float *wh, const float *wo, cons
     out[3] = DistPdf(dist, h, V2(ax, ay));
 }
 LGPU_API float oracle_to_alpha(float r) { return ToAlpha(r); }
+/* texture bilinear fetch at (u, v): RGBA out (known-answer tests) */
+LGPU_API void oracle_kat_texture_bilinear(const float *rgba, int w, int h, float u, float v, float *out) {
+    Real o[4];
+    TexBilinear(rgba, w, h, u, v, o);
+    for (int k = 0; k < 4; ++k) out[k] = o[k];
+}
+/* Sampling::SampleCosineHemisphere (known-answer tests) */
+LGPU_API void oracle_kat_cos_hemisphere(float u0, float u1, float *out) {
+    const V3 w = SampleCosineHemisphere(V2(u0, u1));
+    out[0] = w.x; out[1] = w.y; out[2] = w.z;
+}
 /* Same arguments as the reference-side driver's camera entry point: type 0 pinhole, 1 thin lens,
  * 2 spherical; aperture 0 none, 1 circular, 2 blade (known-answer tests) */
 LGPU_API void oracle_kat_camera_ray(int type, const float *org, const float *xh, const float *yh, const float *zh, float fov,

@@ -8,6 +8,8 @@
  */
 #include <Lambda.h>
 #include <camera/Camera.h>
+#include <image/Texture.h>
+#include <sampling/Sampling.h>
 #include <core/Ray.h>
 #include <core/Spectrum.h>
 #include <sampling/Piecewise.h>
@@ -152,4 +154,22 @@ REF_API void ref_camera_ray(int type, const float *org, const float *xh, const f
     cam->SetFov(fov);
     const Ray r = cam->GenerateRay(u, v, s);
     for (int k = 0; k < 3; ++k) { o[k] = r.o[k]; d[k] = r.d[k]; }
+}
+
+/* texture_t<Colour>::GetPixelUV -> GetPixelUVBilinear (image/Texture.h:71-81, 159-168) over w x h RGBA texels */
+REF_API void ref_texture_bilinear(const float *rgba, int w, int h, float u, float v, float *out) {
+    texture_t<Colour> t((unsigned)w, (unsigned)h);
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const float *p = rgba + 4 * ((size_t)y * w + x);
+            t.SetPixelCoord((unsigned)x, (unsigned)y, Colour(p[0], p[1], p[2], p[3]));
+        }
+    const Colour c = t.GetPixelUV(u, v);   /* interpolation defaults to INTERP_BILINEAR (Texture.h:84) */
+    out[0] = c.r; out[1] = c.g; out[2] = c.b; out[3] = c.a;
+}
+
+/* Sampling::SampleCosineHemisphere (sampling/Sampling.h:15-19) */
+REF_API void ref_cos_hemisphere(float u0, float u1, float *out) {
+    const Vec3 w = Sampling::SampleCosineHemisphere(Vec2(u0, u1));
+    out[0] = w.x; out[1] = w.y; out[2] = w.z;
 }

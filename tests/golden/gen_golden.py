@@ -2,7 +2,8 @@
 
 Loads oracle/_ref/libref_kat.so (built by oracle/build_ref.py from the reference's Fresnel.cpp,
 HenyeyGreenstein.cpp, HomogeneousMedium.cpp, Spectrum.cpp, SPD_Data.cpp, Piecewise.cpp, Camera.cpp,
-Aperture.cpp and TextureEncoding.cpp) and evaluates it on seeded inputs.  Needs the reference tree, so it runs where that exists:
+Aperture.cpp and TextureEncoding.cpp, plus the header-only texture class and sampling routines) and
+evaluates it on seeded inputs.  Needs the reference tree, so it runs where that exists:
 
     python tests/golden/gen_golden.py [reference_root]
 """
@@ -80,6 +81,12 @@ def inputs(seed=7):
                               rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)], 1).astype(F)  # focal, size, blades, offPhi, offTheta
     d["cam_uv"] = rng.uniform(0, 1, (n, 2)).astype(F)
     d["cam_ap_u"] = rng.uniform(0, 1, (n, 8)).astype(F)
+    # image texture bilinear fetch: odd sizes, edge and out-of-range coordinates (clamped)
+    d["tex"] = [rng.uniform(-0.5, 2, (h, w, 4)).astype(F) for h, w in ((1, 1), (3, 5), (8, 8), (17, 6))]
+    uv = rng.uniform(-0.2, 1.2, (40, 2))
+    uv[:6] = [[0, 0], [1, 1], [0.9999, 0.5], [0.5, 0], [1e-7, 1 - 1e-7], [0.25, 0.75]]
+    d["tex_uv"] = uv.astype(F)
+    d["cos_u"] = np.concatenate([rng.uniform(0, 1, (60, 2)), [[0, 0], [1, 0], [0.5, 1]]]).astype(F)
     return d
 
 
@@ -99,7 +106,9 @@ def evaluate(L, prefix, d):
                        ("piecewise2d", [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p], None),
                        ("camera_ray", [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int,
                                        C.c_int, C.c_float, C.c_int, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float,
-                                       C.c_float, C.c_void_p, C.c_void_p, C.c_void_p], None)]:
+                                       C.c_float, C.c_void_p, C.c_void_p, C.c_void_p], None),
+                       ("texture_bilinear", [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p], None),
+                       ("cos_hemisphere", [C.c_float, C.c_float, C.c_void_p], None)]:
         f(n_).argtypes, f(n_).restype = at, rt
     o = {}
     o["fr"] = np.array([f("fr_dielectric")(*r) for r in d["fr_in"]], F)
@@ -158,6 +167,20 @@ def evaluate(L, prefix, d):
                         float(d["cam_uv"][i][1]), _p(np.ascontiguousarray(d["cam_ap_u"][i])), _p(org), _p(dd))
         res.append(np.concatenate([org, dd]))
     o["cam"] = np.array(res, F)
+    for j, t in enumerate(d["tex"]):
+        res = []
+        tc = np.ascontiguousarray(t)
+        for u, v in d["tex_uv"]:
+            out = np.zeros(4, F)
+            f("texture_bilinear")(_p(tc), t.shape[1], t.shape[0], float(u), float(v), _p(out))
+            res.append(out)
+        o["tex_%d" % j] = np.array(res, F)
+    res = []
+    for u in d["cos_u"]:
+        out = np.zeros(3, F)
+        f("cos_hemisphere")(float(u[0]), float(u[1]), _p(out))
+        res.append(out)
+    o["cos_hemi"] = np.array(res, F)
     return o
 
 

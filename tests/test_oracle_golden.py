@@ -1,6 +1,7 @@
 """The oracle's restatement against golden vectors computed by the reference renderer's own code
 (tests/golden/ref_kat.npz, made by tests/golden/gen_golden.py from the reference's Fresnel,
-Henyey-Greenstein, homogeneous-medium, spectrum, piecewise-distribution, camera and aperture units).
+Henyey-Greenstein, homogeneous-medium, spectrum, piecewise-distribution, camera, aperture, texture
+and sampling code).
 
 Tolerance: 2e-6 relative (1e-7 absolute) -- both sides are the same float arithmetic built with
 -ffp-contract=off; the slack covers libm differences between hosts.  Indices are exact.
@@ -87,6 +88,14 @@ def test_cameras(oracle_out, gold):
     # the thin lens with an aperture moves the origin off the camera position
     moved = (d["cam_kind"][:, 0] == 1) & (d["cam_kind"][:, 1] > 0) & (d["cam_lens"][:, 1] > 0.01)
     assert np.all(np.linalg.norm(gold["cam"][moved, :3] - d["cam_org"][moved], axis=1) > 1e-4)
+
+
+def test_texture_bilinear_and_cosine_hemisphere(oracle_out, gold):
+    """Image-texture fetch (GetPixelUVBilinear with its clamping) and cosine-hemisphere sampling."""
+    _, o, _ = oracle_out
+    for k in [k for k in gold if k.startswith("tex_")]:
+        close(o[k], gold[k])
+    close(o["cos_hemi"], gold["cos_hemi"])
 
 
 def _smits_tables():
