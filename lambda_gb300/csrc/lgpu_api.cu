@@ -213,6 +213,13 @@ bool validate_scene(const HostScene &H, std::string &why) {
     const DeviceScene &S = H.S;
     if (!check_bvh(H, S.root, S.use_tlas != 0, why)) return false;
     const size_t fp = H.fpool.size();
+    for (size_t t = 0; t < H.maskCond.size(); ++t) {   /* masked-aperture distributions */
+        if (H.maskCond[t] < 0) continue;
+        const size_t w = (size_t)H.texW[t], h = (size_t)H.texH[t];
+        if ((size_t)H.maskCond[t] + h * (2 * w + 2) > fp || H.maskMarg[t] < 0 || (size_t)H.maskMarg[t] + 2 * h + 1 > fp) {
+            why = "aperture mask distribution"; return false;
+        }
+    }
     for (size_t i = 0; i < H.objects.size(); ++i) {
         const DObject &o = H.objects[i];
         if (o.mesh < 0 || (size_t)o.mesh >= H.meshes.size() || o.material < 0 || (size_t)o.material >= H.mats.size()) { why = "object refs"; return false; }

@@ -2,6 +2,7 @@
 light tree matches the oracle's ManyLightSampler build."""
 import re
 
+import numpy as np
 import pytest
 
 from lambda_gb300 import configs
@@ -67,5 +68,23 @@ def test_image_texture_needs_a_scene_texture(lg):
 
 def test_image_texture_scene_compiles(lg):
     sb, cams, opts = configs.cornell_inverse(16, 16, 1, tex_res=8)
+    rc, rep = lg.scene_check(sb)
+    assert rc == 0, rep
+
+
+@pytest.mark.parametrize("kind", ["disc", "zero", "one_texel", "negative"])
+def test_aperture_mask_textures_compile(lg, kind):
+    """Masked-aperture distributions are built at commit for flagged textures, including an
+    all-zero mask (uniform fallback of Piecewise1D), a 1x1 mask and negative red (|red|)."""
+    sb, cam, opts = configs.cornell(8, 8, 1)
+    if kind == "one_texel":
+        m = np.ones((1, 1, 4), np.float32)
+    else:
+        yy, xx = np.mgrid[0:12, 0:9]
+        m = np.zeros((12, 9, 4), np.float32)
+        if kind != "zero":
+            m[..., 0] = ((xx - 4) ** 2 + (yy - 6) ** 2 < 16) * (-1.0 if kind == "negative" else 1.0)
+    sb.texture(m, aperture_mask=True)
+    sb.texture(np.ones((4, 4, 4), np.float32))          # an unflagged texture next to it
     rc, rep = lg.scene_check(sb)
     assert rc == 0, rep
