@@ -2571,6 +2571,8 @@ static V2 ApertureSample(const Oracle *o, const lgpu_camera_desc &c, Sampler &s)
     }
     case LGPU_APERTURE_MASKED: {   /* MaskedAperture::Sample_p (Aperture.cpp:33-36) */
         const Real ux = s.Get1D(), uy = s.Get1D();
+        if (!o || c.aperture_mask < 0 || c.aperture_mask >= (int)o->masks.size() || !o->masks[c.aperture_mask])
+            return V2(0, 0);   /* unreachable from oracle_render, which rejects such a camera */
         Real pdf;
         const V2 p = o->masks[c.aperture_mask]->SampleContinuous(V2(ux, uy), &pdf);
         return V2(p.x * size - size * (Real).5, p.y * size - size * (Real).5);
@@ -2665,6 +2667,9 @@ LGPU_API void oracle_tree_info(void *h, float *out) {
 LGPU_API int oracle_render(void *handle, const lgpu_camera_desc *cam, const lgpu_render_opts *opt,
                            const uint64_t *ids, uint64_t n, float *film, float *path_out, int threads) {
     Oracle *o = (Oracle *)handle;
+    if (cam->type == LGPU_CAMERA_THIN_LENS && cam->aperture == LGPU_APERTURE_MASKED &&
+        (cam->aperture_mask < 0 || cam->aperture_mask >= (int)o->masks.size() || !o->masks[cam->aperture_mask]))
+        return 1;   /* as the GPU library: a masked aperture needs a texture committed with aperture_mask */
     g_ns = (opt->spectral_mode == LGPU_SPECTRAL_HERO4) ? 4 : 3;
     for (auto &m : o->sc.media) m.Prepare();
     const uint64_t total = ids ? n : (uint64_t)opt->width * opt->height * opt->spp;

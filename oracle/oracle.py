@@ -97,14 +97,16 @@ class Oracle:
         """Full frame: returns the film (H, W, 4) = summed RGB + count."""
         film = np.zeros((opts.height, opts.width, 4), np.float32)
         cam = camera.desc()
-        lib().oracle_render(self._h, C.byref(cam), C.byref(opts), None, 0, _p(film), None, threads)
+        if lib().oracle_render(self._h, C.byref(cam), C.byref(opts), None, 0, _p(film), None, threads):
+            raise ValueError("oracle rejected the camera")
         return film
 
     def render_paths(self, camera, opts, path_ids, threads=0):
         ids = np.ascontiguousarray(path_ids, np.uint64)
         outp = np.zeros((len(ids), 4), np.float32)
         cam = camera.desc()
-        lib().oracle_render(self._h, C.byref(cam), C.byref(opts), _p(ids), len(ids), None, _p(outp), threads)
+        if lib().oracle_render(self._h, C.byref(cam), C.byref(opts), _p(ids), len(ids), None, _p(outp), threads):
+            raise ValueError("oracle rejected the camera")
         return outp
 
     def tree_info(self):

@@ -69,3 +69,15 @@ def test_camera_rays_unit_and_centred(kind):
         # the centre of the film looks down z; a circular aperture of size 0 sits at -size/2 = 0
         np.testing.assert_allclose(d, cam.z, atol=1e-5)
         np.testing.assert_allclose(o, cam.origin, atol=1e-6)
+
+
+def test_masked_aperture_needs_flagged_texture():
+    oracle, L = _lib()
+    sb, cam0, opts = configs.cornell(4, 4, 1)
+    t = sb.texture(np.ones((4, 4, 4), np.float32))           # not flagged: no distribution
+    o = oracle.Oracle(sb)
+    cam = Camera(cam0.origin, cam0.origin + cam0.z, kind="thin_lens", aperture="masked", aperture_size=0.1,
+                 aperture_mask=t)
+    with pytest.raises(ValueError):
+        o.render_paths(cam, opts, np.arange(4, dtype=np.uint64))
+    o.close()
