@@ -81,3 +81,30 @@ def test_masked_aperture_needs_flagged_texture():
     with pytest.raises(ValueError):
         o.render_paths(cam, opts, np.arange(4, dtype=np.uint64))
     o.close()
+
+
+def test_camera_descriptor_fields():
+    """scene.Camera fills lgpu_camera_desc: kind and aperture codes, lens values, spherical offsets,
+    and an orthonormal frame with z towards the target."""
+    from lambda_gb300 import abi
+    c = Camera((1.0, 2.0, 3.0), (1.0, 2.0, 10.0), fov=0.7, kind="thin_lens", focal_length=2.5, aperture="blade",
+               aperture_size=0.2, blades=5)
+    d = c.desc()
+    assert (d.type, d.aperture, d.blades) == (abi.CAMERA_THIN_LENS, abi.APERTURE_BLADE, 5)
+    assert d.focal_length == pytest.approx(2.5) and d.aperture_size == pytest.approx(0.2) and d.fov == pytest.approx(0.7)
+    x, y, z = (np.array(v) for v in (d.x_hat, d.y_hat, d.z_hat))
+    np.testing.assert_allclose(z, [0, 0, 1], atol=1e-6)
+    np.testing.assert_allclose([x @ y, y @ z, z @ x], 0, atol=1e-6)
+    s = Camera((0, 0, 0), (0, 0, 1), kind="spherical", offset_phi=0.25, offset_theta=-0.5).desc()
+    assert s.type == abi.CAMERA_SPHERICAL and s.offset_phi == pytest.approx(0.25) and s.offset_theta == pytest.approx(-0.5)
+    assert Camera((0, 0, 0), (0, 0, 1)).desc().type == abi.CAMERA_PINHOLE
+
+
+def test_texture_mask_flag_in_scene_descriptor():
+    sb, _cam, _opts = configs.cornell(4, 4, 1)
+    a = sb.texture(np.ones((2, 3, 4), np.float32))
+    b = sb.texture(np.ones((5, 4, 3), np.float32), aperture_mask=True)
+    d = sb.desc()
+    assert d.num_textures == 2
+    assert (d.textures[a].aperture_mask, d.textures[a].width, d.textures[a].height) == (0, 3, 2)
+    assert (d.textures[b].aperture_mask, d.textures[b].width, d.textures[b].height) == (1, 4, 5)
