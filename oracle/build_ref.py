@@ -24,9 +24,18 @@ UNITS = ["shading/Fresnel.cpp", "shading/media/HenyeyGreenstein.cpp", "shading/m
 UNIT_FLAGS = {"camera/Aperture.cpp": ["-mbmi2"]}
 
 
+def _has_bmi2():
+    try:
+        return "bmi2" in pathlib.Path("/proc/cpuinfo").read_text().split()
+    except OSError:
+        return False
+
+
 def build(ref_root="/root/reference", force=False):
+    """Returns the library path, or None where it cannot be built here (no reference tree, or a
+    host without the BMI2 instructions the reference's texture class needs)."""
     src = pathlib.Path(ref_root) / "src"
-    if not src.is_dir():
+    if not src.is_dir() or not _has_bmi2():
         return None
     if LIB.exists() and not force and LIB.stat().st_mtime >= (HERE / "ref_kat.cpp").stat().st_mtime:
         return LIB
