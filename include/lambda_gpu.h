@@ -463,7 +463,10 @@ LGPU_API int lgpu_adjoint(lgpu_context *ctx, const lgpu_camera_desc *camera, con
  *     library (one copy per device), holding a pool of at most LGPU_NOALLOC_MAX_SLOTS paths in
  *     flight; any n streams through that pool.  opts->pool_slots = 0 uses the whole pool, values
  *     above LGPU_NOALLOC_MAX_SLOTS are rejected with LGPU_ERR_INVALID_ARG;
- *   - the wavefront kernels always run (kernel_mode MEGAKERNEL is rejected); no traversal counters.
+ *   - the wavefront kernels always run, and they are the MIS volumetric integrator: kernel_mode
+ *     MEGAKERNEL and every integrator other than LGPU_INTEGRATOR_GPU_MISVOLPATH are rejected with
+ *     LGPU_ERR_INVALID_ARG; no traversal counters (lgpu_get_stats reports this call's paths,
+ *     iterations, queries and launches, without stage timings).
  * The call issues its work on `stream` and returns when it has finished.  The first call on a
  * device also looks up the array's address (cudaGetSymbolAddress) and may make the driver load
  * the kernels' code, so make it before any stream capture or allocation-free region starts.

@@ -1750,6 +1750,8 @@ LGPU_API int lgpu_render_paths_noalloc(lgpu_context *c, const lgpu_camera_desc *
     if (!path_ids_dev || !path_out_dev) return fail(c, LGPU_ERR_INVALID_ARG, "null path buffers");
     if (o->kernel_mode == LGPU_KERNEL_MEGAKERNEL)
         return fail(c, LGPU_ERR_INVALID_ARG, "lgpu_render_paths_noalloc runs the wavefront kernels only");
+    if (o->integrator != LGPU_INTEGRATOR_GPU_MISVOLPATH)   /* the wavefront is the MIS volumetric integrator */
+        return fail(c, LGPU_ERR_INVALID_ARG, "lgpu_render_paths_noalloc runs LGPU_INTEGRATOR_GPU_MISVOLPATH only");
     if (o->pool_slots < 0 || o->pool_slots > LGPU_NOALLOC_MAX_SLOTS) {
         char msg[160];
         std::snprintf(msg, sizeof(msg), "pool_slots %d is outside the fixed scratch pool (1..%d slots, 0 = all)",
@@ -1801,22 +1803,54 @@ LGPU_API int lgpu_render_paths_noalloc(lgpu_context *c, const lgpu_camera_desc *
     W.free_count = counts + 2 * LG_NSEG;
     auto resume = [&](int m, int mode) { return hero ? wave_resume_4_0(W, m, mode, st) : wave_resume_3_0(W, m, mode, st); };
 
+    /* a failure leaves no work of this call queued against the shared array once the lock is
+     * released: drain the stream first (its own error, if any, is already being reported) */
+    auto failed = [&](int code, cudaError_t err, const char *what) {
+        cudaStreamSynchronize(st);
+        return err != cudaSuccess ? cuda_fail(c, err, what) : fail(c, code, what);
+    };
+    c->stats.trace_ms = c->stats.shade_ms = c->stats.spawn_ms = 0;
+    for (int k = 0; k < 6; ++k) { c->stats.stage_ms[k] = 0; c->stats.resumed[k] = 0; }
+    c->stats.traced = c->stats.spawned = c->stats.launches = 0;
+    c->stats.last_render_ms = 0;
     e = cudaMemsetAsync(counts, 0, (2 * LG_NSEG + 2) * sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(W.next_path, 0, sizeof(unsigned long long), st);
     W.queue_in = nullptr; W.queue_out = qa; W.count_out = ca;
     if (e == cudaSuccess) e = resume((int)slots, 2);   /* fill the pool */
-    if (e != cudaSuccess) return cuda_fail(c, e, "wavefront start");
+    if (e != cudaSuccess) return failed(0, e, "wavefront start");
     int h_count[LG_NSEG];
     int iters = 0;
+    /* Every iteration advances each path in flight by at least one query, and one path issues at
+     * most (max_bounces + 1) x 2048 + 512 of them (per bounce: an extension query plus up to four
+     * transmittance loops of at most 256 segments; at most 256 null-surface crossings per path).
+     * So n paths need at most n times that many iterations, whatever the pool size: the bound
+     * only catches a state machine that stopped making progress, never a long call. */
+    const uint64_t per_path = (uint64_t)(o->max_bounces + 1) * 2048u + 512u;
+    const uint64_t max_iters = n > ~0ull / per_path ? ~0ull : n * per_path;
+    uint64_t launches = 1;
     for (;;) {
         e = cudaMemcpyAsync(h_count, ca, sizeof(h_count), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) return cuda_fail(c, e, "wavefront");
+        if (e != cudaSuccess) return failed(0, e, "wavefront");
         int m = 0;
         W.seg_off[0] = 0;
         for (int k = 0; k < LG_NSEG; ++k) { m += h_count[k]; W.seg_off[k + 1] = m; }
-        if (m <= 0) break;
-        if (++iters > 100000) return fail(c, LGPU_ERR_TIMEOUT, "wavefront did not drain");
+        if (m <= 0) {
+            /* no path in flight: done, unless every path of the last spawn ended inside it (e.g.
+             * max_bounces = 0) and ids are left unstarted; then spawn into the whole pool again */
+            unsigned long long next = 0;
+            e = cudaMemcpyAsync(&next, W.next_path, sizeof(next), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return failed(0, e, "wavefront");
+            if (next >= n) break;
+            if (++iters > max_iters) return failed(LGPU_ERR_TIMEOUT, cudaSuccess, "wavefront did not drain");
+            W.queue_in = nullptr; W.queue_out = qa; W.count_out = ca;
+            e = resume((int)slots, 2);
+            if (e != cudaSuccess) return failed(0, e, "wavefront restart");
+            launches += 2;
+            continue;
+        }
+        if (++iters > max_iters) return failed(LGPU_ERR_TIMEOUT, cudaSuccess, "wavefront did not drain");
         e = cudaMemsetAsync(cb, 0, LG_NSEG * sizeof(int), st);
         W.queue_in = qa; W.queue_out = qb; W.count_out = cb;
         if (e == cudaSuccess) e = wave_trace_3_0(W, m, st);
@@ -1828,14 +1862,20 @@ LGPU_API int lgpu_render_paths_noalloc(lgpu_context *c, const lgpu_camera_desc *
             W.queue_in = qa + (size_t)k * W0.cap;
             W.cap_in = 0;
             e = resume(nk, 0);
+            c->stats.resumed[k] += (uint64_t)nk;
+            launches += 1;
             W = W0;
         }
         if (e == cudaSuccess) e = resume(m, 1);   /* new paths into the freed slots */
-        if (e != cudaSuccess) return cuda_fail(c, e, "wavefront iteration");
+        if (e != cudaSuccess) return failed(0, e, "wavefront iteration");
+        c->stats.traced += (uint64_t)m;
+        launches += 3;
         std::swap(qa, qb);
         std::swap(ca, cb);
     }
     c->stats.paths = n;
+    c->stats.spawned = n;
+    c->stats.launches = launches;
     c->stats.iterations = (uint32_t)iters;
     c->stats.pool_slots = (uint32_t)slots;
     return LGPU_OK;

@@ -70,6 +70,36 @@ def test_noalloc_volume_hero_small_pool(gpu_lib):
     _check(sb, cam, opts, 48 * 27 * 4)
 
 
+def test_noalloc_paths_ending_in_spawn(gpu_lib):
+    # max_bounces = 0: every path ends inside the spawn that starts it, so the pool empties after
+    # each spawn and the call must start the next pool of ids itself (NaN marks unwritten paths)
+    from lambda_gb300 import configs
+    sb, cam, opts = configs.cornell(40, 40, 2)
+    opts.max_bounces = 0
+    opts.pool_slots = 700
+    _check(sb, cam, opts, 40 * 40 * 2)
+
+
+def test_noalloc_rejects_other_integrators(gpu_lib):
+    torch = pytest.importorskip("torch")
+    import lambda_gb300 as lg
+    from lambda_gb300 import abi, configs
+    L = _bind()
+    sb, cam, opts = configs.cornell(16, 16, 1)
+    opts.integrator = abi.INTEGRATOR_PATH
+    r = lg.Renderer(sb)
+    try:
+        ids = torch.arange(16 * 16, dtype=torch.int64, device="cuda")
+        out = torch.zeros((16 * 16, 4), dtype=torch.float32, device="cuda")
+        desc = cam.desc()
+        rc = L.lgpu_render_paths_noalloc(r.handle, C.byref(desc), C.byref(opts), C.c_void_p(ids.data_ptr()),
+                                         16 * 16, C.c_void_p(out.data_ptr()), None)
+        assert rc == abi.ERR_INVALID_ARG
+        assert "GPU_MISVOLPATH" in L.lgpu_last_error(r.handle).decode()
+    finally:
+        r.close()
+
+
 def test_noalloc_rejects_pool_beyond_scratch(gpu_lib):
     torch = pytest.importorskip("torch")
     import lambda_gb300 as lg
