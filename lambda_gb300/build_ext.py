@@ -15,12 +15,15 @@ CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 LIB = OUT / "liblambda_gpu.so"
 # (source, extra defines, object name); the render megakernel is built once per variant
+# Render kernels: one unit per (spectral mode, counter variant, part); part 1 MIS megakernel, 2 wavefront
+# resume/spawn, 3 trace + closest-hit batches + film kernels (RGB3 only), 4 adjoint (RGB3, no counters),
+# 5 megakernel of the other integrators.
+_PARTS = [(ns, cnt, part) for ns in (3, 4) for cnt in (0, 1) for part in (1, 2, 3, 4, 5)
+          if (part != 3 or ns == 3) and (part != 4 or (ns == 3 and cnt == 0))]
 SOURCES = [("lgpu_api.cu", [], "lgpu_api"), ("lgpu_compile.cu", [], "lgpu_compile"),
-           ("lgpu_lighttree.cpp", [], "lgpu_lighttree"),
-           ("lgpu_render.cu", ["-DLGPU_NS=3", "-DLGPU_COUNT=0"], "render_3_0"),
-           ("lgpu_render.cu", ["-DLGPU_NS=3", "-DLGPU_COUNT=1"], "render_3_1"),
-           ("lgpu_render.cu", ["-DLGPU_NS=4", "-DLGPU_COUNT=0"], "render_4_0"),
-           ("lgpu_render.cu", ["-DLGPU_NS=4", "-DLGPU_COUNT=1"], "render_4_1")]
+           ("lgpu_lighttree.cpp", [], "lgpu_lighttree")] + [
+    ("lgpu_render.cu", ["-DLGPU_NS=%d" % ns, "-DLGPU_COUNT=%d" % cnt, "-DLGPU_PART=%d" % part],
+     "render_%d_%d_p%d" % (ns, cnt, part)) for ns, cnt, part in _PARTS]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -56,8 +59,12 @@ def build(force=False, verbose=False, defines=(), out_dir=None):
             raise RuntimeError("nvcc failed on %s:\n%s\n%s" % (src, r.stdout, r.stderr))
         return obj, r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(compile_one, SOURCES))
+    # the slowest units first (resume/spawn, the other integrators, the adjoint, the MIS megakernel),
+    # so the pool's last jobs are short ones
+    rank = {"-DLGPU_PART=2": 0, "-DLGPU_PART=5": 1, "-DLGPU_PART=4": 2, "-DLGPU_PART=1": 3}
+    order = sorted(SOURCES, key=lambda sp: min([rank.get(d, 9) for d in sp[1]] + [9]))
+    with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 8)) as ex:
+        results = list(ex.map(compile_one, order))
     objs = [str(o) for o, _ in results]
     if verbose:
         for _, log in results:

@@ -49,6 +49,11 @@ cudaError_t launch_render_3_0(const LaunchArgs &a);
 cudaError_t launch_render_3_1(const LaunchArgs &a);
 cudaError_t launch_render_4_0(const LaunchArgs &a);
 cudaError_t launch_render_4_1(const LaunchArgs &a);
+/* the integrators other than GPU_MISVOLPATH (launch_render_* forwards to these) */
+cudaError_t launch_render_other_3_0(const LaunchArgs &a);
+cudaError_t launch_render_other_3_1(const LaunchArgs &a);
+cudaError_t launch_render_other_4_0(const LaunchArgs &a);
+cudaError_t launch_render_other_4_1(const LaunchArgs &a);
 inline cudaError_t launch_render(const LaunchArgs &a) {
     if (a.hero) return a.count ? launch_render_4_1(a) : launch_render_4_0(a);
     return a.count ? launch_render_3_1(a) : launch_render_3_0(a);

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "lgpu_camera.cuh"
 #include "lgpu_integrator.cuh"
@@ -21,6 +22,15 @@
 #endif
 #ifndef LGPU_COUNT
 #define LGPU_COUNT 0
+#endif
+/* LGPU_PART selects the kernels of this translation unit, so that the build compiles them in
+ * parallel: 1 megakernel of the MIS volumetric integrator, 2 wavefront resume/spawn, 3 wavefront
+ * trace, closest-hit batches and film kernels, 4 path-replay adjoint, 5 megakernel of the other
+ * integrators (path, volumetric path, direct lighting, normal and depth passes); undefined: all. */
+#ifndef LGPU_PART
+#define LG_PART(k) 1
+#else
+#define LG_PART(k) (LGPU_PART == (k))
 #endif
 
 namespace lg {
@@ -41,7 +51,9 @@ __device__ __forceinline__ void hero_to_rgb(const Spec<NS> &L, const Lambda4 &la
     out[2] = 0.055648f * xyz[0] - 0.204043f * xyz[1] + 1.057311f * xyz[2];
 }
 
-template <int NS, bool COUNT>
+#if LG_PART(1) || LG_PART(5)
+/* MIS: the MIS volumetric integrator only (part 1); otherwise the integrator named by rp (part 5) */
+template <int NS, bool COUNT, bool MIS>
 __global__ void __launch_bounds__(128) k_render(const __grid_constant__ DeviceScene S, const __grid_constant__ CamParams cam, const __grid_constant__ RenderParams rp, float4 *film,
                                                 float4 *paths_out, const uint64_t *ids, uint64_t n,
                                                 unsigned long long *counters) {
@@ -74,13 +86,16 @@ __global__ void __launch_bounds__(128) k_render(const __grid_constant__ DeviceSc
         camera_ray(cam, S.fpool, x, y, rng, o, d);
         Tracer<NS, COUNT> T{S, rng, lam, &st};
         Spec<NS> L;
-        switch (rp.integrator) {
-        case LGPU_INTEGRATOR_PATH: L = T.Li_path(o, d, rp.max_bounces, rp.min_bounces); break;
-        case LGPU_INTEGRATOR_VOLPATH: L = T.Li_volpath(o, d, rp.max_bounces, rp.min_bounces); break;
-        case LGPU_INTEGRATOR_DIRECT: L = T.Li_direct(o, d); break;
-        case LGPU_INTEGRATOR_NORMAL: L = T.Li_pass(o, d, true); break;
-        case LGPU_INTEGRATOR_DEPTH: L = T.Li_pass(o, d, false); break;
-        default: L = T.Li(o, d, rp.max_bounces, rp.min_bounces); break;
+        if (MIS) {
+            L = T.Li(o, d, rp.max_bounces, rp.min_bounces);
+        } else {
+            switch (rp.integrator) {
+            case LGPU_INTEGRATOR_PATH: L = T.Li_path(o, d, rp.max_bounces, rp.min_bounces); break;
+            case LGPU_INTEGRATOR_VOLPATH: L = T.Li_volpath(o, d, rp.max_bounces, rp.min_bounces); break;
+            case LGPU_INTEGRATOR_DIRECT: L = T.Li_direct(o, d); break;
+            case LGPU_INTEGRATOR_NORMAL: L = T.Li_pass(o, d, true); break;
+            default: L = T.Li_pass(o, d, false); break;   /* LGPU_INTEGRATOR_DEPTH */
+            }
         }
         hero_to_rgb<NS>(L, lam, rgb);
         /* w = random numbers drawn: a control-flow fingerprint of the path */
@@ -123,7 +138,9 @@ __global__ void __launch_bounds__(128) k_render(const __grid_constant__ DeviceSc
     }
 }
 
-#if LGPU_NS == 3 && LGPU_COUNT == 0
+#endif  /* parts 1, 5 */
+
+#if LGPU_NS == 3 && LGPU_COUNT == 0 && LG_PART(4)
 /* Path-replay adjoint: one thread per path of the frame, the forward path recomputed with the same
  * random numbers while gradients of the image loss are accumulated (Tracer::Li_adj). */
 __global__ void __launch_bounds__(128) k_adjoint(const __grid_constant__ DeviceScene S, const __grid_constant__ CamParams cam,
@@ -160,6 +177,9 @@ cudaError_t launch_adjoint(const DeviceScene &S, const CamParams &cam, const Ren
     k_adjoint<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S, cam, rp, A, n);
     return cudaGetLastError();
 }
+#endif  /* part 4 */
+
+#if LGPU_NS == 3 && LGPU_COUNT == 0 && LG_PART(3)
 
 /* Closest-hit queries for a ray batch (Scene::Intersect restated; tnear = 0, tfar = inf). */
 __global__ void k_intersect(const __grid_constant__ DeviceScene S, const float4 *rays, uint4 *hits, float2 *uvs, uint64_t n) {
@@ -179,21 +199,54 @@ __global__ void k_intersect(const __grid_constant__ DeviceScene S, const float4 
 }
 #endif
 
-/* Each (spectral mode, counter) variant is compiled in its own translation unit so the four
+/* Each (spectral mode, counter) variant is compiled in its own translation units so the four
  * megakernel instantiations build in parallel: LGPU_NS and LGPU_COUNT select the variant. */
 #define LG_CAT2(a, b, c) a##b##_##c
 #define LG_CAT(a, b, c) LG_CAT2(a, b, c)
 
+#if LG_PART(1)
 cudaError_t LG_CAT(launch_render_, LGPU_NS, LGPU_COUNT)(const LaunchArgs &a) {
+    if (a.rp.integrator != LGPU_INTEGRATOR_GPU_MISVOLPATH) return LG_CAT(launch_render_other_, LGPU_NS, LGPU_COUNT)(a);
     const int bs = 128;
     const uint64_t blocks = (a.n + bs - 1) / bs;
     if (blocks == 0) return cudaSuccess;
-    k_render<LGPU_NS, LGPU_COUNT != 0><<<(unsigned)blocks, bs, 0, a.stream>>>(a.S, a.cam, a.rp, a.film, a.paths_out, a.ids,
-                                                                            a.n, a.counters);
+    k_render<LGPU_NS, LGPU_COUNT != 0, true><<<(unsigned)blocks, bs, 0, a.stream>>>(a.S, a.cam, a.rp, a.film, a.paths_out,
+                                                                                  a.ids, a.n, a.counters);
     return cudaGetLastError();
+}
+#endif  /* part 1 */
+#if LG_PART(5)
+cudaError_t LG_CAT(launch_render_other_, LGPU_NS, LGPU_COUNT)(const LaunchArgs &a) {
+    const int bs = 128;
+    const uint64_t blocks = (a.n + bs - 1) / bs;
+    if (blocks == 0) return cudaSuccess;
+    k_render<LGPU_NS, LGPU_COUNT != 0, false><<<(unsigned)blocks, bs, 0, a.stream>>>(a.S, a.cam, a.rp, a.film, a.paths_out,
+                                                                                   a.ids, a.n, a.counters);
+    return cudaGetLastError();
+}
+#endif  /* part 5 */
+
+/* Blocks of a device-driven launch: enough to fill every SM at the kernel's occupancy. */
+template <typename K>
+static int resident_grid(K kernel, int block, size_t smem) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+    return std::max(1, sms * std::max(1, per_sm));
+}
+/* Launch set-up is per device (grid sizes depend on the device's SM count; function attributes
+ * are set in the current device's context).  Two threads setting up the same device at once
+ * compute the same values, so plain atomics suffice. */
+constexpr int LG_MAX_DEVICES = 64;
+static inline int current_device() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev >= 0 && dev < LG_MAX_DEVICES ? dev : 0;
 }
 
 /* ---------------------------------------------------------------- wavefront kernels */
+#if LG_PART(2)
 template <int NS, bool COUNT>
 __device__ __forceinline__ void wave_save(Wave<NS, COUNT> &w, PHot<NS> &s) {
     s.key = w.rng.key;
@@ -321,16 +374,6 @@ static __global__ void k_wave_advance(WaveArgs W, int n_max, int fresh) {
     *W.free_count = 0;
 }
 
-/* Blocks of a device-driven launch: enough to fill every SM at the kernel's occupancy. */
-template <typename K>
-static int resident_grid(K kernel, int block, size_t smem) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
-    return std::max(1, sms * std::max(1, per_sm));
-}
-
 cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, int start_new, cudaStream_t st) {
     constexpr bool C = LGPU_COUNT != 0;
 #ifdef LGPU_NO_STAGE
@@ -338,14 +381,19 @@ cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, 
 #else
     const size_t smem = 128 * sizeof(PHot<LGPU_NS>);
 #endif
-    static int grid_resume = 0, grid_spawn = 0;
-    if (!grid_resume) {
+    static std::atomic<int> grids_resume[LG_MAX_DEVICES], grids_spawn[LG_MAX_DEVICES];
+    const int dev = current_device();
+    int grid_resume = grids_resume[dev].load(std::memory_order_acquire);
+    int grid_spawn = grids_spawn[dev].load(std::memory_order_acquire);
+    if (!grid_resume || !grid_spawn) {
         for (auto k : {k_wave_resume<LGPU_NS, C, false>, k_wave_resume<LGPU_NS, C, true>})
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         for (auto k : {k_wave_spawn<LGPU_NS, C, false>, k_wave_spawn<LGPU_NS, C, true>})
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         grid_resume = resident_grid(k_wave_resume<LGPU_NS, C, true>, 128, smem);
         grid_spawn = resident_grid(k_wave_spawn<LGPU_NS, C, true>, 128, smem);
+        grids_spawn[dev].store(grid_spawn, std::memory_order_release);
+        grids_resume[dev].store(grid_resume, std::memory_order_release);
     }
     /* n < 0: device-driven launch over a fixed resident grid (sizes read on the device) */
     if (start_new) {
@@ -365,8 +413,9 @@ cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, 
 }
 size_t LG_CAT(wave_state_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PHot<LGPU_NS>); }
 size_t LG_CAT(wave_cold_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PCold<LGPU_NS>); }
+#endif  /* part 2 */
 
-#if LGPU_NS == 3
+#if LGPU_NS == 3 && LG_PART(3)
 /* Answer every queued query: closest hit (Scene::Intersect) or occlusion (rtcOccluded1). */
 template <bool COUNT, int BS, bool DEV>
 __global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveArgs W, int n) {
@@ -417,8 +466,13 @@ __global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveA
  * n == 0: set-up of the resident grid only.  block: 64, 128, 256 or 512 threads. */
 template <int BS>
 static cudaError_t trace_launch(const WaveArgs &W, int n, cudaStream_t st) {
-    static int grid = 0;
-    if (!grid) grid = resident_grid(k_wave_trace<LGPU_COUNT != 0, BS, true>, BS, 0);   /* n == 0: set-up only */
+    static std::atomic<int> grids[LG_MAX_DEVICES];
+    const int dev = current_device();
+    int grid = grids[dev].load(std::memory_order_acquire);
+    if (!grid) {   /* n == 0: set-up only */
+        grid = resident_grid(k_wave_trace<LGPU_COUNT != 0, BS, true>, BS, 0);
+        grids[dev].store(grid, std::memory_order_release);
+    }
     if (n == 0) return cudaSuccess;
     if (n < 0) k_wave_trace<LGPU_COUNT != 0, BS, true><<<grid, BS, 0, st>>>(W, 0);
     else k_wave_trace<LGPU_COUNT != 0, BS, false><<<(n + BS - 1) / BS, BS, 0, st>>>(W, n);
@@ -434,7 +488,7 @@ cudaError_t LG_CAT(wave_trace_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, c
 }
 #endif
 
-#if LGPU_NS == 3 && LGPU_COUNT == 0
+#if LGPU_NS == 3 && LGPU_COUNT == 0 && LG_PART(3)
 /* film[pixel] += (sum of the pixel's spp path radiances, spp): Film::AddSample for a whole tile. */
 __global__ void k_film_reduce(const float4 *paths, float4 *film, uint64_t first_px, uint64_t n_px, int spp) {
     const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
