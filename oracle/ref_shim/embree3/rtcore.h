@@ -1,8 +1,8 @@
 /*
- * Declaration-only stand-in for Embree 3's public header, used only to compile a handful of the
- * reference renderer's translation units (Fresnel, Henyey-Greenstein, homogeneous medium, spectrum,
- * piecewise distributions) for golden vectors.  None of those units calls Embree; the types only
- * have to exist because core/Ray.h and core/Scene.h name them.  TEST INFRASTRUCTURE ONLY.
+ * Stand-in for Embree 3's public header (the library is absent), for the reference-renderer builds in
+ * oracle/_ref only.  TEST INFRASTRUCTURE ONLY.  It declares the types and the calls the reference
+ * makes (src/core/Ray.h, Scene.h/.cpp, TriangleMesh.cpp, Instance.cpp); oracle/ref_shim/rtcore_bvh.cpp
+ * implements them for the integrator library, and the golden-vector library links none of them.
  */
 #pragma once
 #include <cstddef>
@@ -27,7 +27,7 @@ struct RTCIntersectContext { RTCIntersectContextFlags flags; void *filter; unsig
 struct RTCCollision { unsigned geomID0, primID0, geomID1, primID1; };
 typedef void (*RTCCollideFunc)(void *, RTCCollision *, unsigned);
 inline void rtcInitIntersectContext(RTCIntersectContext *c) { c->flags = RTC_INTERSECT_CONTEXT_FLAG_INCOHERENT; c->filter = nullptr; }
-/* declared so the headers parse; never defined or called by the golden-vector library */
+/* implemented in rtcore_bvh.cpp (integrator library only) */
 RTCDevice rtcNewDevice(const char *);
 RTCScene rtcNewScene(RTCDevice);
 void rtcSetSceneFlags(RTCScene, RTCSceneFlags);
