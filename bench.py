@@ -12,8 +12,10 @@ is additionally flushed between timed steps.
           in-kernel by a separate counting render of the same frame, plus ray and hit records) over
           its own time, taken from CUDA events the library records around every launch on the render
           stream; all kernels are listed under roofline.kernels
-  cpu_baseline  the CPU oracle (restatement of the reference integrator) on this host's cores over
-          a bounded stratified sample of the same frame
+  cpu_baseline  the reference renderer's own CPU integrator and tile renderer (built from its sources
+          with Embree replaced, oracle/build_ref.py) on this host's cores over a bounded sample of
+          tiles of the same frame -- or the CPU oracle where the reference cannot be built -- plus
+          the per-path agreement of the GPU with it on 20,000 seeded paths of the frame (parity)
 
 --impl reference runs that CPU path alone with all host threads on the same config and metric.
 Multi-GPU (torchrun, N > 1): replicas -- every rank renders its own frame (seed = rank); no
@@ -130,32 +132,80 @@ class ClockSampler:
         return res
 
 
-def cpu_baseline(sb, cam, opts, seconds, threads=0):
-    """Oracle throughput on a stratified pixel sample at full spp (bounded to ~`seconds`)."""
-    from oracle.oracle import Oracle
-    o = Oracle(sb)
+def _tile_sample(W, H, n):
+    """n of the frame's 16 x 16 tiles (row-major tile index), evenly strided over the frame."""
+    total = ((W + 15) // 16) * ((H + 15) // 16)
+    n = max(1, min(total, n))
+    return (np.arange(n) * (total / n)).astype(np.int64).astype(np.int32), total
+
+
+def cpu_baseline(sb, cam, opts, seconds, threads=0, gpu=None, parity_paths=20000):
+    """CPU throughput on a bounded sample of the same frame (about `seconds` of work) and, when `gpu`
+    (a Renderer of the same scene) is given, per-path agreement of the GPU with the CPU path.
+
+    kind "reference": the reference renderer's own code (RenderMosaic + TileRenderers::UniformSpp +
+    MISVolumetricPathIntegrator::Li, built from its sources by oracle/build_ref.py, Embree replaced by
+    oracle/ref_shim) over an evenly strided sample of 16 x 16 tiles at full spp, on `threads` host
+    threads.  kind "port": the CPU oracle (the restatement) over a stratified pixel sample, where the
+    reference cannot be built."""
+    from oracle import reference
     W, H, spp = opts.width, opts.height, opts.spp
     threads = threads or os.cpu_count()
+    ids_par = None
+    if gpu is not None:
+        rng = np.random.RandomState(99)
+        ids_par = np.sort(rng.choice(W * H * spp, min(parity_paths, W * H * spp), replace=False)).astype(np.uint64)
+    if reference.available():
+        ref = reference.Reference(sb)
+        calib, total = _tile_sample(W, H, 2 * threads)
+        t0 = time.perf_counter()
+        ref.render_tiles(cam, opts, calib, threads=threads)
+        rate = len(calib) / max(time.perf_counter() - t0, 1e-6)   # tiles per second
+        tiles, total = _tile_sample(W, H, int(max(4, rate * seconds)))
+        t0 = time.perf_counter()
+        film = ref.render_tiles(cam, opts, tiles, threads=threads)
+        dt = time.perf_counter() - t0
+        n_paths = float(film[..., 3].sum())
+        res = {"value": n_paths / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "reference",
+               "sample": "%d of %d 16x16 tiles (every %.1fth, full %d spp) = %d path samples in %.1f s, by the "
+                         "reference's TileRenderers::UniformSpp + MISVolumetricPathIntegrator::Li"
+                         % (len(tiles), total, total / len(tiles), spp, n_paths, dt)}
+        cpu_paths = ref.render_paths(cam, opts, ids_par, threads=threads) if ids_par is not None else None
+        ref.close()
+    else:
+        from oracle.oracle import Oracle
+        o = Oracle(sb)
 
-    def ids_for(npix, offset=0):
-        step = max(1, (W * H) // npix)
-        px = (np.arange(npix, dtype=np.uint64) * step + offset) % (W * H)
-        return (px[:, None] * spp + np.arange(spp, dtype=np.uint64)[None, :]).reshape(-1)
+        def ids_for(npix, offset=0):
+            step = max(1, (W * H) // npix)
+            px = (np.arange(npix, dtype=np.uint64) * step + offset) % (W * H)
+            return (px[:, None] * spp + np.arange(spp, dtype=np.uint64)[None, :]).reshape(-1)
 
-    calib = ids_for(max(1, 2048 // spp * 8), 7)
-    t0 = time.perf_counter()
-    o.render_paths(cam, opts, calib, threads=threads)
-    dt = time.perf_counter() - t0
-    rate = len(calib) / max(dt, 1e-6)
-    npix = int(max(16, min(W * H, rate * seconds / spp)))
-    ids = ids_for(npix, 13)
-    t0 = time.perf_counter()
-    o.render_paths(cam, opts, ids, threads=threads)
-    dt = time.perf_counter() - t0
-    o.close()
-    return {"value": len(ids) / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d of %d pixels (stratified, every %dth) x %d spp = %d path samples in %.1f s"
-                      % (npix, W * H, max(1, (W * H) // npix), spp, len(ids), dt)}
+        calib = ids_for(max(1, 2048 // spp * 8), 7)
+        t0 = time.perf_counter()
+        o.render_paths(cam, opts, calib, threads=threads)
+        rate = len(calib) / max(time.perf_counter() - t0, 1e-6)
+        npix = int(max(16, min(W * H, rate * seconds / spp)))
+        ids = ids_for(npix, 13)
+        t0 = time.perf_counter()
+        o.render_paths(cam, opts, ids, threads=threads)
+        dt = time.perf_counter() - t0
+        res = {"value": len(ids) / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+               "why_not_reference": reference.unavailable_reason(),
+               "sample": "%d of %d pixels (stratified, every %dth) x %d spp = %d path samples in %.1f s"
+                         % (npix, W * H, max(1, (W * H) // npix), spp, len(ids), dt)}
+        cpu_paths = o.render_paths(cam, opts, ids_par, threads=threads) if ids_par is not None else None
+        o.close()
+    if ids_par is not None:
+        got = gpu.render_paths(cam, opts, ids_par)
+        a, b = got[:, :3].astype(np.float64), cpu_paths[:, :3].astype(np.float64)
+        err = np.abs(a - b) / np.maximum(np.maximum(np.abs(a), np.abs(b)), 1e-6)
+        ok = np.all((err <= 1e-4) | (np.abs(a - b) <= 1e-6), axis=1)
+        same = ok & (got[:, 3] == cpu_paths[:, 3])
+        res["parity"] = {"paths": int(len(ids_par)), "agree": float(same.mean()),
+                         "criterion": "rgb within 1e-4 relative (1e-6 floor) and equal random numbers drawn",
+                         "against": res["kind"], "differing_ids": [int(i) for i in ids_par[~same][:10]]}
+    return res
 
 
 def replica_seed(rank):
@@ -440,7 +490,7 @@ def main():
         K, W_ = args.steps, args.warmup
         vals = []
         for i in range(W_ + K):
-            cb = cpu_baseline(sb, cam, opts, max(2.0, min(args.cpu_seconds, 240.0 / (K + W_))))
+            cb = cpu_baseline(sb, cam, opts, max(2.0, min(args.cpu_seconds, 150.0 / (K + W_))))
             if i >= W_:
                 vals.append(cb["value"])
         v = float(np.median(vals))
@@ -543,7 +593,7 @@ def main():
             "step_ms": float(np.mean(kernel_ms))}
     cpu = None
     if not args.no_cpu:
-        cpu = cpu_baseline(sb, cam, opts, args.cpu_seconds)
+        cpu = cpu_baseline(sb, cam, opts, args.cpu_seconds, gpu=r)
     cfg["l2"] = "scene data > L2 and a 256 MiB buffer is written between timed steps"
     cfg["width"], cfg["height"], cfg["spp"] = W, H, spp
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -172,6 +172,79 @@ def cornell(width=256, height=256, spp=16, max_depth=8, subdiv=3, light_intensit
     return sb, cam, opts
 
 
+# ------------------------------------------------------------------ parity scene: every graph node
+def node_zoo(width=48, height=48, spp=4, max_depth=6, light_strategy=abi.LIGHT_STRATEGY_POWER):
+    """Closed box whose materials route through every shader-graph node kind the GPU compiles
+    (value noise, checker, vector maths with all four operators, dot, cross, magnitude, separate
+    XYZ / RGBA, merge XYZ / RGBA, surface information, constant spectrum, sqrt and power), a
+    Beckmann microfacet sphere with noise-driven roughness, a specular mirror sphere, an Oren-Nayar
+    wall, lit by a quad emitter, a point light and a spotlight through the power-CDF light sampler
+    (light_strategy) -- a parity scene for the branches the benchmark scenes leave out."""
+    sb = SceneBuilder()
+    sb.light_strategy = light_strategy
+    # floor albedo: r = value noise * 0.7, g = checker (scaled by sqrt), b = |normal x (0,0,1)| and
+    # the surface normal through vector maths; every output feeds the albedo so nothing is folded away
+    vnoise = sb.node("VALUE_NOISE", [6.0])
+    chk = sb.node("CHECKER", [8.0])
+    nrm = sb.node("SURFACE_INFO")
+    k07, k2, k3, k05 = (sb.node("SCALAR", [v]) for v in (0.7, 2.0, 3.0, 0.5))
+    r = sb.node("MATHS", inputs={0: out(vnoise), 1: out(k07)}, op=abi.MATHS_MULTIPLY)
+    sq = sb.node("MATHS", inputs={0: out(chk), 1: 0.0}, op=abi.MATHS_SQRT)
+    g = sb.node("MATHS", inputs={0: out(sq), 1: out(k05)}, op=abi.MATHS_MULTIPLY)
+    axis = sb.node("VECTOR3", [0.0, 0.0, 1.0])
+    cr = sb.node("CROSS_PRODUCT", inputs={0: out(nrm), 1: out(axis)})
+    mag = sb.node("VECTOR_MAGNITUDE", inputs={0: out(cr)})
+    vsum = sb.node("VECTOR_MATHS", inputs={0: out(nrm), 1: out(axis)}, op=abi.MATHS_ADD)
+    vdif = sb.node("VECTOR_MATHS", inputs={0: out(vsum), 1: (0.25, 0.5, 0.25, 0)}, op=abi.MATHS_SUBTRACT)
+    vmul = sb.node("VECTOR_MATHS", inputs={0: out(vdif), 1: (0.5, 0.5, 0.5, 0)}, op=abi.MATHS_MULTIPLY)
+    vdiv = sb.node("VECTOR_MATHS", inputs={0: out(vmul), 1: (2.0, 4.0, 8.0, 1)}, op=abi.MATHS_DIVIDE)
+    sep = sb.node("SEPARATE_XYZ", inputs={0: out(vdiv)})
+    dot = sb.node("DOT_PRODUCT", inputs={0: out(nrm), 1: out(vdiv)})
+    b0 = sb.node("MATHS", inputs={0: out(mag), 1: out(sep, 1)}, op=abi.MATHS_ADD)
+    b1 = sb.node("MATHS", inputs={0: out(b0), 1: out(dot)}, op=abi.MATHS_SUBTRACT)
+    bpow = sb.node("MATHS", inputs={0: out(b1), 1: out(k2)}, op=abi.MATHS_POWER)
+    b = sb.node("MATHS", inputs={0: out(bpow), 1: out(k3)}, op=abi.MATHS_DIVIDE)
+    rgba = sb.node("MERGE_RGBA", inputs={0: out(r), 1: out(g), 2: out(b), 3: 1.0})
+    chan = sb.node("SEPARATE_RGBA", inputs={0: out(rgba)})
+    xyz = sb.node("MERGE_XYZ", inputs={0: out(chan, 0), 1: out(chan, 1), 2: out(chan, 2)})
+    floor = sb.node("BXDF_LAMBERTIAN", inputs={0: out(xyz)})
+    # Beckmann sphere, roughness 0.1 + 0.4 * value noise; mirror sphere; Oren-Nayar back wall with
+    # a constant-spectrum albedo
+    rn = sb.node("VALUE_NOISE", [3.0])
+    rs = sb.node("MATHS", inputs={0: out(rn), 1: 0.4}, op=abi.MATHS_MULTIPLY)
+    rough = sb.node("MATHS", inputs={0: out(rs), 1: 0.1}, op=abi.MATHS_ADD)
+    beck = sb.node("BXDF_MICROFACET_R", [abi.DIST_BECKMANN, 1.5], {0: (0.9, 0.7, 0.5, 1), 1: out(rough)})
+    mirror = sb.node("BXDF_SPECULAR_R", [1.5], {0: (0.95, 0.95, 0.95, 1)})
+    spec = sb.node("SPECTRUM", [0.6, 0.5, 0.4])
+    onw = sb.node("BXDF_OREN_NAYAR_R", inputs={0: out(spec), 1: math.radians(30.0)})
+    white = sb.node("BXDF_LAMBERTIAN", inputs={0: (0.73, 0.73, 0.73, 1)})
+    black = sb.node("BXDF_LAMBERTIAN", inputs={0: (0.0, 0.0, 0.0, 1)})
+    m_floor, m_beck, m_mirror, m_on, m_white = (sb.material(x) for x in (floor, beck, mirror, onw, white))
+    uv = [(0, 0), (0, 4), (4, 4), (4, 0)]
+    walls = [((-1, -1, -1), (-1, -1, 1), (1, -1, 1), (1, -1, -1), m_floor),
+             ((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1), m_white),
+             ((-1, -1, 1), (-1, 1, 1), (1, 1, 1), (1, -1, 1), m_on),
+             ((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1), m_white),
+             ((1, -1, -1), (1, -1, 1), (1, 1, 1), (1, 1, -1), m_white)]
+    for p0, p1, p2, p3, m in walls:
+        v, t = quad(p0, p1, p2, p3)
+        sb.obj(sb.mesh(v, t, uvs=uv), m)
+    for centre, m in (((-0.4, -0.65, 0.2), m_beck), ((0.45, -0.7, -0.1), m_mirror)):
+        sv, st, sn, stg, suv = latlong_sphere(16, 24, 0.3)
+        sb.obj(sb.mesh(sv + np.asarray(centre, np.float32), st, sn, stg, suv), m)
+    h = 0.15
+    lv, lt = quad((-h, 0.999, -h), (h, 0.999, -h), (h, 0.999, h), (-h, 0.999, h))
+    m_light = sb.material(black, light=len(sb.lights))
+    lobj = sb.obj(sb.mesh(lv, lt), m_light)
+    sb.light_mesh(lobj, blackbody_emission(sb, 5000.0), 30.0)
+    warm = out(sb.node("RGB", [1.0, 0.8, 0.6]))
+    sb.light_point((0.6, 0.5, -0.5), warm, 1.5)
+    sb.light_spot((-0.5, 0.9, 0.3), (0.3, -1.0, 0.1), math.radians(35.0), math.radians(25.0), warm, 4.0)
+    cam = Camera((0, 0, -3.4), (0, -0.2, 0), fov=0.75)
+    opts = abi.render_opts(width, height, spp, max_depth)
+    return sb, cam, opts
+
+
 # ------------------------------------------------------------------ config: inverse rendering
 def inverse_cameras(n=8, radius=3.0, spread=0.6):
     """n pinhole cameras on an arc of the ring of the given radius around the box centre, facing

@@ -115,14 +115,13 @@ def _shader_graph_m1(text):
     return text[:after] + "\n\n" + specs + "\n" + body + "\n" + text[after:]
 
 
-# (unit, id, reason, old, new); `old` must occur exactly once unless EDIT_COUNT names another count
-EDIT_COUNT = {"M3": 3}
+# (unit, id, reason, old, new[, count]); `old` must occur exactly `count` times (default once)
 EDITS = [
     ("shading/graph/ShaderGraph.h", "M2", "string literal bound to constexpr char * (ill-formed in C++11 and later)",
      'template<class T> constexpr char *getSocketTag = "Null";',
      'template<class T> constexpr char const *getSocketTag = "Null";'),
     ("image/Texture.cpp", "M3", "std::powf is not declared by libstdc++",
-     "std::powf", "std::pow"),
+     "std::powf", "std::pow", 3),
     ("sampling/SampleShifter.h", "S1", "accessor for the pixel index set by TileRenderers (counter-based sampler key)",
      "\t\tReal Shift(const Real _point, const unsigned _dimensionIndex) const;",
      "\t\tReal Shift(const Real _point, const unsigned _dimensionIndex) const;\n\n"
@@ -161,6 +160,21 @@ EDITS = [
      "if (nl != l) { const Vec3 hp = hit.point, hn = hit.normalS; hit.point = sampPoint; hit.normalS = sampNormal;"
      " lightDistPdf = _scene.lightSampler->Pdf(event, nl); hit.point = hp; hit.normalS = hn; }"),
     ("integrators/MISVolumetricPathIntegrator.cpp", "B32", "escape at bounce 0 dereferences a null environment light",
+     "if (bounces == 0) L += ((Light*)_scene.envLight)->Le(r) * beta;",
+     "if (bounces == 0 && _scene.envLight) L += ((Light*)_scene.envLight)->Le(r) * beta;"),
+    ("integrators/PathIntegrator.cpp", "B7", "light-tree pdf evaluated at the next hit instead of the shading point",
+     "Real lightDistPdf = 1;", "Real lightDistPdf = 1; const Vec3 sampPoint = hit.point, sampNormal = hit.normalS;"),
+    ("integrators/PathIntegrator.cpp", "B7", "light-tree pdf evaluated at the next hit instead of the shading point",
+     "if (nl != l) lightDistPdf = _scene.lightSampler->Pdf(event, nl);",
+     "if (nl != l) { const Vec3 hp = hit.point, hn = hit.normalS; hit.point = sampPoint; hit.normalS = sampNormal;"
+     " lightDistPdf = _scene.lightSampler->Pdf(event, nl); hit.point = hp; hit.normalS = hn; }"),
+    ("integrators/VolumetricPathIntegrator.cpp", "B7", "light-tree pdf evaluated at the next hit instead of the shading point",
+     "Real lightDistPdf = 1;", "Real lightDistPdf = 1; const Vec3 sampPoint = hit.point, sampNormal = hit.normalS;", 2),
+    ("integrators/VolumetricPathIntegrator.cpp", "B7", "light-tree pdf evaluated at the next hit instead of the shading point",
+     "if (nl != l) lightDistPdf = _scene.lightSampler->Pdf(event, nl);",
+     "if (nl != l) { const Vec3 hp = hit.point, hn = hit.normalS; hit.point = sampPoint; hit.normalS = sampNormal;"
+     " lightDistPdf = _scene.lightSampler->Pdf(event, nl); hit.point = hp; hit.normalS = hn; }", 2),
+    ("integrators/VolumetricPathIntegrator.cpp", "B32", "escape at bounce 0 dereferences a null environment light",
      "if (bounces == 0) L += ((Light*)_scene.envLight)->Le(r) * beta;",
      "if (bounces == 0 && _scene.envLight) L += ((Light*)_scene.envLight)->Le(r) * beta;"),
     ("lighting/ManyLightSampler.cpp", "B8", "RecursivePDF: right-child probability 1 - IR instead of 1 - pdfs[0]",
@@ -282,10 +296,12 @@ def prepare(ref_root=None, force=False):
     sg = COPY / "shading" / "graph" / "ShaderGraph.h"
     sg.write_text(_shader_graph_m1(sg.read_text(encoding="latin-1")), encoding="latin-1")
     log = ["M1 shading/graph/ShaderGraph.h: Socket::GetAs specialisations and GetAsSpectrum moved to namespace scope"]
-    for unit, tag, why, old, new in EDITS:
+    for edit in EDITS:
+        unit, tag, why, old, new = edit[:5]
+        want = edit[5] if len(edit) > 5 else 1
         p = COPY / unit
         t = p.read_text(encoding="latin-1")
-        n, want = t.count(old), EDIT_COUNT.get(tag, 1)
+        n = t.count(old)
         if n != want:
             raise RuntimeError("edit %s in %s: expected %d match(es), found %d" % (tag, unit, want, n))
         p.write_text(t.replace(old, new), encoding="latin-1")

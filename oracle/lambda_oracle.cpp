@@ -608,7 +608,7 @@ static Val EvalOutput(const Graph &g, int node, int out, const ScatterEvent &ev)
     case LGPU_NODE_VECTOR3: r.v[0] = d.params[0]; r.v[1] = d.params[1]; r.v[2] = d.params[2]; break;
     case LGPU_NODE_RGB: r.v[0] = d.params[0]; r.v[1] = d.params[1]; r.v[2] = d.params[2]; r.v[3] = 1; break;
     case LGPU_NODE_SPECTRUM: { const Real rgb[3] = {d.params[0], d.params[1], d.params[2]}; r.s = FromRGB(rgb, false); break; }
-    case LGPU_NODE_BLACKBODY: r.s = MakeBlackbody(AsReal(in(0).pull()), (unsigned)d.params[0]); break;
+    case LGPU_NODE_BLACKBODY: r.s = MakeBlackbody(in(0).real(), (unsigned)d.params[0]); break;
     case LGPU_NODE_SURFACE_INFO: r.v[0] = ev.hit->normalS.x; r.v[1] = ev.hit->normalS.y; r.v[2] = ev.hit->normalS.z; break;
     case LGPU_NODE_IMAGE_TEXTURE: {   /* ImageTextureInput::GetColour / GetScalar (GraphInputs.cpp:128-136) */
         const int ti = (int)d.params[0];
@@ -619,16 +619,16 @@ static Val EvalOutput(const Graph &g, int node, int out, const ScatterEvent &ev)
         break;
     }
     case LGPU_NODE_SEPARATE_XYZ: {        /* B14: every output reads input 0 */
-        const V3 v = AsVec3(in(0).pull());
+        const V3 v = in(0).vec3();
         r.v[0] = out == 0 ? v.x : (out == 1 ? v.y : v.z);
         break;
     }
-    case LGPU_NODE_SEPARATE_RGBA: { Real c[4]; AsColour(in(0).pull(), c); r.v[0] = c[out]; break; }
-    case LGPU_NODE_MERGE_XYZ: r.v[0] = AsReal(in(0).pull()); r.v[1] = AsReal(in(1).pull()); r.v[2] = AsReal(in(2).pull()); break;
-    case LGPU_NODE_MERGE_RGBA: for (int i = 0; i < 4; ++i) r.v[i] = AsReal(in(i).pull()); break;
+    case LGPU_NODE_SEPARATE_RGBA: { Real c[4]; in(0).colour(c); r.v[0] = c[out]; break; }
+    case LGPU_NODE_MERGE_XYZ: r.v[0] = in(0).real(); r.v[1] = in(1).real(); r.v[2] = in(2).real(); break;
+    case LGPU_NODE_MERGE_RGBA: for (int i = 0; i < 4; ++i) r.v[i] = in(i).real(); break;
     case LGPU_NODE_MATHS: {
-        const Real a = AsReal(in(0).pull());
-        const Real b = (d.op == LGPU_MATHS_SQRT) ? 0 : AsReal(in(1).pull());
+        const Real a = in(0).real();
+        const Real b = (d.op == LGPU_MATHS_SQRT) ? 0 : in(1).real();
         switch (d.op) {
         case LGPU_MATHS_ADD: r.v[0] = a + b; break;
         case LGPU_MATHS_SUBTRACT: r.v[0] = a - b; break;
@@ -640,7 +640,7 @@ static Val EvalOutput(const Graph &g, int node, int out, const ScatterEvent &ev)
         break;
     }
     case LGPU_NODE_VECTOR_MATHS: {
-        const V3 a = AsVec3(in(0).pull()), b = AsVec3(in(1).pull());
+        const V3 a = in(0).vec3(), b = in(1).vec3();
         V3 o;
         switch (d.op) {
         case LGPU_MATHS_ADD: o = a + b; break;
@@ -652,9 +652,9 @@ static Val EvalOutput(const Graph &g, int node, int out, const ScatterEvent &ev)
         r.v[0] = o.x; r.v[1] = o.y; r.v[2] = o.z;
         break;
     }
-    case LGPU_NODE_DOT_PRODUCT: r.v[0] = Dot(AsVec3(in(0).pull()), AsVec3(in(1).pull())); break;
-    case LGPU_NODE_CROSS_PRODUCT: { const V3 o = Cross(AsVec3(in(0).pull()), AsVec3(in(1).pull())); r.v[0] = o.x; r.v[1] = o.y; r.v[2] = o.z; break; }
-    case LGPU_NODE_VECTOR_MAGNITUDE: r.v[0] = AsVec3(in(0).pull()).Magnitude(); break;
+    case LGPU_NODE_DOT_PRODUCT: r.v[0] = Dot(in(0).vec3(), in(1).vec3()); break;
+    case LGPU_NODE_CROSS_PRODUCT: { const V3 o = Cross(in(0).vec3(), in(1).vec3()); r.v[0] = o.x; r.v[1] = o.y; r.v[2] = o.z; break; }
+    case LGPU_NODE_VECTOR_MAGNITUDE: r.v[0] = in(0).vec3().Magnitude(); break;
     case LGPU_NODE_PERLIN_NOISE: case LGPU_NODE_VALUE_NOISE: case LGPU_NODE_OCTAVE_NOISE:
     case LGPU_NODE_CHECKER: case LGPU_NODE_VORONOI:
         r.v[0] = ev.mediumInteraction ? Noise3D(g, node, ev.hit->point) : Noise2D(g, node, ev.hit->uv);

@@ -440,14 +440,15 @@ std::shared_ptr<Integrator> make_integrator(const lgpu_render_opts &o, Sampler *
     }
 }
 
-template <class F> void parallel(uint64_t n, int threads, F &&f) {
+/* f(0 .. n-1) on `threads` threads, handed out dynamically in chunks of `grain` */
+template <class F> void parallel(uint64_t n, int threads, uint64_t grain, F &&f) {
     if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<uint64_t> next(0);
     auto work = [&]() {
         for (;;) {
-            const uint64_t b = next.fetch_add(64);
+            const uint64_t b = next.fetch_add(grain);
             if (b >= n) return;
-            for (uint64_t i = b; i < std::min(n, b + 64); ++i) f(i);
+            for (uint64_t i = b; i < std::min(n, b + grain); ++i) f(i);
         }
     };
     std::vector<std::thread> pool;
@@ -488,7 +489,7 @@ int render_tiles(RefScene &R, const lgpu_camera_desc *cd, const lgpu_render_opts
     } else {
         for (int i = 0; i < (int)mosaic.tiles.size(); ++i) todo.push_back(i);
     }
-    parallel(todo.size(), threads, [&](uint64_t k) { TileRenderers::UniformSpp(&mosaic.tiles[todo[k]]); });
+    parallel(todo.size(), threads, 1, [&](uint64_t k) { TileRenderers::UniformSpp(&mosaic.tiles[todo[k]]); });
     for (int y = 0; y < o->height; ++y)
         for (int x = 0; x < o->width; ++x) {
             const FilmPixel &p = film.filmData.GetPixelCoord(x, y);
@@ -528,7 +529,7 @@ __attribute__((visibility("default"))) int ref_render(void *h, const lgpu_camera
     }
     const int W = o->width, H = o->height;
     const Real xi = (Real)1 / W, yi = (Real)1 / H;
-    parallel(n, threads, [&](uint64_t i) {
+    parallel(n, threads, 64, [&](uint64_t i) {
         CounterSampler s;
         s.seed = o->seed;
         s.offset = o->sample_offset;
