@@ -5,7 +5,7 @@ These are published colourimetry data sets.  They are read from the reference's
 src/core/SPD_Data.cpp so that the GPU module, the CPU oracle and the reference use bit-identical
 constants.  Run by hand when the reference tree is available:
 
-    python lambda_gb300/csrc/gen_spectral_tables.py /root/reference/src/core/SPD_Data.cpp
+    python lambda_gb300/csrc/gen_spectral_tables.py <reference_root>/src/core/SPD_Data.cpp
 """
 import re
 import sys
@@ -59,4 +59,6 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src/core/SPD_Data.cpp")
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: gen_spectral_tables.py <path of the reference's src/core/SPD_Data.cpp>")
+    main(sys.argv[1])

@@ -72,7 +72,7 @@ def build(ref_root=None, force=False):
     tree, or a host without the BMI2 instructions the reference's texture class needs)."""
     root = reference_root(ref_root)
     if root is None or not (root / "src").is_dir() or not _has_bmi2():
-        return None
+        return LIB if LIB.exists() and _has_bmi2() and not force else None   # built earlier on this host
     src = root / "src"
     if LIB.exists() and not force and LIB.stat().st_mtime >= (HERE / "ref_kat.cpp").stat().st_mtime:
         return LIB

@@ -5,7 +5,7 @@ HenyeyGreenstein.cpp, HomogeneousMedium.cpp, Spectrum.cpp, SPD_Data.cpp, Piecewi
 Aperture.cpp and TextureEncoding.cpp, plus the header-only texture class and sampling routines) and
 evaluates it on seeded inputs.  Needs the reference tree, so it runs where that exists:
 
-    python tests/golden/gen_golden.py [reference_root]
+    python tests/golden/gen_golden.py <reference_root>     (or LAMBDA_REFERENCE_ROOT)
 """
 import ctypes as C
 import pathlib
@@ -184,11 +184,11 @@ def evaluate(L, prefix, d):
     return o
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
     from oracle import build_ref
-    lib = build_ref.build(ref_root)
+    lib = build_ref.build(ref_root, force=True)
     if lib is None:
-        raise SystemExit("reference tree not found at %s" % ref_root)
+        raise SystemExit("reference tree not found (pass it or set LAMBDA_REFERENCE_ROOT)")
     L = C.CDLL(str(lib))
     d = inputs()
     o = evaluate(L, "ref_", d)
