@@ -32,18 +32,23 @@ def nvcc():
     return p
 
 
-def _flags():
-    return ["-O3", "-std=c++17", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
+def _flags(fmad=False):
+    """Device code is compiled without multiply-add contraction (-fmad=false), as the host code and the
+    CPU checkers are (-ffp-contract=off): every a * b + c rounds twice, as in the reference, so a
+    path's sampling decisions are the reference's own.  With contraction, 2-3 % of the paths of the
+    full-size scenes took another branch on a last-bit difference."""
+    return ["-O3", "-std=c++17", "-lineinfo", *ARCH, "-fmad=%s" % ("true" if fmad else "false"),
+            "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
             "-I" + str(CSRC), "-I" + str(HERE.parent / "include")]
 
 
-def build(force=False, verbose=False, defines=(), out_dir=None):
-    """Compile into lambda_gb300/_build (or out_dir, for tuning variants built with extra
-    -D defines such as LGPU_RESUME_MINB=5 or LGPU_NO_STAGE)."""
+def build(force=False, verbose=False, defines=(), out_dir=None, extra_flags=(), fmad=False):
+    """Compile into lambda_gb300/_build (or out_dir, for variants built with extra -D defines such
+    as LGPU_RESUME_MINB=5 or LGPU_NO_STAGE, extra nvcc flags, or fmad=True for contraction)."""
     out = pathlib.Path(out_dir) if out_dir else OUT
     lib_path = out / LIB.name
     out.mkdir(parents=True, exist_ok=True)
-    deps = list(CSRC.glob("*")) + [HERE.parent / "include" / "lambda_gpu.h"]
+    deps = list(CSRC.glob("*")) + [HERE.parent / "include" / "lambda_gpu.h", pathlib.Path(__file__)]
     newest = max(p.stat().st_mtime for p in deps)
     if lib_path.exists() and not force and lib_path.stat().st_mtime >= newest:
         return lib_path
@@ -51,7 +56,7 @@ def build(force=False, verbose=False, defines=(), out_dir=None):
     def compile_one(spec):
         src, defs, name = spec
         obj = out / (name + ".o")
-        cmd = [nvcc(), *_flags(), *defs, *["-D" + d for d in defines], "-c", str(CSRC / src), "-o", str(obj)]
+        cmd = [nvcc(), *_flags(fmad), *defs, *["-D" + d for d in defines], *extra_flags, "-c", str(CSRC / src), "-o", str(obj)]
         if verbose and src.endswith(".cu"):
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)

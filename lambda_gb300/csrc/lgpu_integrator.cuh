@@ -386,16 +386,22 @@ struct Tracer {
     /* ManyLightSampler::ImportanceMeasure (ManyLightSampler.cpp:305-326), useSplits = true:
      *   theta  = acos(delta . axis), thetaU = atan(r / d), thetaDash = max(theta - thetaO - thetaU, 0)
      *   I = cos(max(thetaI - thetaU, 0)) * E / d^2 * cos(thetaDash)   if thetaDash < thetaE (= pi/2)
-     * evaluated with cosine/sine identities instead of acos / atan / cos (same value to ~1e-6
-     * relative).  The reference's NaN cases are kept: a cone cosine outside [-1, 1] gives 0, a normal
-     * cosine outside [-1, 1] gives NaN. */
+     * evaluated with cosine/sine identities instead of acos / atan / cos.  The reference's angles come
+     * from acos of the rounded dot products, so the dot products are rounded as the reference rounds
+     * them (products, then sums) and the sines are taken as sqrt((1 - c)(1 + c)), which keeps full
+     * relative precision for cosines near 1, where acos is ill-conditioned.  The reference's NaN
+     * cases are kept: a cone cosine outside [-1, 1] gives 0, a normal cosine outside [-1, 1] NaN. */
+    static __device__ __forceinline__ float dot_rn(float3 a, float3 b) {
+        return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+    }
+    static __device__ __forceinline__ float sin_of_cos(float c) { return sqrtf(smax(0.f, (1.f - c) * (1.f + c))); }
     __device__ __forceinline__ float importance(float3 p, float3 nS, const DLNode &n) {
         float3 delta = n.center - p;
-        const float d2 = dot(delta, delta);
+        const float d2 = dot_rn(delta, delta);
         const float dd = sqrtf(d2);
         const float invD = 1.f / dd;
-        delta = delta * invD;
-        const float cosT = dot(delta, n.axis);
+        delta = make_float3(__fmul_rn(delta.x, invD), __fmul_rn(delta.y, invD), __fmul_rn(delta.z, invD));
+        const float cosT = dot_rn(delta, n.axis);
         if (!(cosT >= -1.f && cosT <= 1.f)) return 0.f;
         const float tU = (n.diag * .5f) * invD;
         const float cosU = 1.f / sqrtf(1.f + tU * tU), sinU = tU * cosU;
@@ -403,17 +409,14 @@ struct Tracer {
         const float sinA = n.sinO * cosU + n.cosO * sinU;
         float cosDash = 1.f;
         if (!(sinA < 0.f || cosT >= cosA)) {               /* theta > a (and a <= pi) */
-            const float sinT = sqrtf(smax(0.f, 1.f - cosT * cosT));
-            cosDash = cosT * cosA + sinT * sinA;
+            cosDash = cosT * cosA + sin_of_cos(cosT) * sinA;
             if (!(cosDash > 0.f)) return 0.f;               /* thetaDash >= thetaE = pi/2 */
         }
-        const float cosI = dot(delta, nS);
+        const float cosI = dot_rn(delta, nS);
         if (!(cosI >= -1.f && cosI <= 1.f)) return __int_as_float(0x7fc00000);
         float cosTerm = 1.f;
-        if (cosI < cosU) {                                  /* thetaI > thetaU */
-            const float sinI = sqrtf(smax(0.f, 1.f - cosI * cosI));
-            cosTerm = cosI * cosU + sinI * sinU;
-        }
+        if (cosI < cosU)                                    /* thetaI > thetaU */
+            cosTerm = cosI * cosU + sin_of_cos(cosI) * sinU;
         return (cosTerm * n.power) / d2 * cosDash;
     }
     __device__ LRef tree_light_ref(int idx) {

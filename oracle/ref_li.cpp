@@ -51,7 +51,9 @@
 #include <shading/media/HomogeneousMedium.h>
 
 #include <atomic>
+#include <iostream>
 #include <memory>
+#include <streambuf>
 #include <string>
 #include <thread>
 #include <vector>
@@ -505,9 +507,19 @@ extern "C" {
 
 __attribute__((visibility("default"))) const char *ref_last_error() { return g_err.c_str(); }
 
+/* ManyLightSampler::Commit reports progress on std::cout; callers of this library own stdout (a
+ * benchmark prints one JSON line there), so the scene build runs with std::cout discarded. */
+struct NullBuf : std::streambuf {
+    int overflow(int c) override { return c; }
+};
+
 __attribute__((visibility("default"))) void *ref_create(const lgpu_scene_desc *d) {
+    static NullBuf sink;
+    std::streambuf *keep = std::cout.rdbuf(&sink);
     RefScene *R = new RefScene();
-    if (!load(*R, d)) { delete R; return nullptr; }
+    const bool ok = load(*R, d);
+    std::cout.rdbuf(keep);
+    if (!ok) { delete R; return nullptr; }
     return R;
 }
 

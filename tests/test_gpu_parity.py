@@ -1,8 +1,10 @@
 """GPU path vs CPU oracle on the same seeded inputs (per path, per ray, per image).
 
-Criteria (from the reference's integrator run with the same counter-based RNG):
-  * per-path radiance within 1e-4 relative on >= 99 % of paths; the rest are divergences where a
-    1-ulp difference (FMA contraction on the GPU) flips a sampling decision;
+Criteria (the oracle reproduces the reference's own integrators path by path, see
+tests/test_oracle_reference.py):
+  * per-path radiance within 1e-4 relative and the same number of random numbers drawn on
+    >= 99.9 % of paths (the device code is built without multiply-add contraction, so it rounds as
+    the reference does; the rest differ where a math-library result differs in its last bit);
   * closest-hit primitive ids agree on >= 99.99 % of rays and t within 1e-5 relative;
   * images: per-pixel means agree within a 3-sigma band of the per-pixel sample variance.
 """
@@ -34,7 +36,7 @@ def test_cornell_rgb_paths(gpu_lib, mode):
     g, o = _render_both(gpu_lib, sb, cam, opts, 48 * 48 * 4)
     frac, ok = path_agreement(g, o)
     assert np.isfinite(g).all()
-    assert frac >= 0.99, "per-path agreement %.5f" % frac
+    assert frac >= 0.999, "per-path agreement %.5f" % frac
 
 
 @MODES
@@ -45,7 +47,7 @@ def test_cornell_hero_paths(gpu_lib, mode):
     opts.spectral_mode = abi.SPECTRAL_HERO4
     g, o = _render_both(gpu_lib, sb, cam, opts, 32 * 32 * 4)
     frac, _ = path_agreement(g, o)
-    assert frac >= 0.99, "per-path agreement %.5f" % frac
+    assert frac >= 0.999, "per-path agreement %.5f" % frac
 
 
 @MODES
@@ -55,7 +57,7 @@ def test_terrain_small_paths(gpu_lib, mode):
     opts.kernel_mode = mode
     g, o = _render_both(gpu_lib, sb, cam, opts, 64 * 36 * 4)
     frac, _ = path_agreement(g, o)
-    assert frac >= 0.99, "per-path agreement %.5f" % frac
+    assert frac >= 0.999, "per-path agreement %.5f" % frac
 
 
 @MODES
@@ -65,7 +67,7 @@ def test_volume_small_paths(gpu_lib, mode):
     opts.kernel_mode = mode
     g, o = _render_both(gpu_lib, sb, cam, opts, 48 * 27 * 4)
     frac, _ = path_agreement(g, o)
-    assert frac >= 0.99, "per-path agreement %.5f" % frac
+    assert frac >= 0.999, "per-path agreement %.5f" % frac
 
 
 @MODES
@@ -113,7 +115,7 @@ def test_inverse_cornell_texture_medium_paths(gpu_lib, mode):
         g, o = _render_both(gpu_lib, sb, cam, opts, 40 * 40 * 4)
         frac, _ = path_agreement(g, o)
         assert np.isfinite(g).all()
-        assert frac >= 0.99, "per-path agreement %.5f" % frac
+        assert frac >= 0.999, "per-path agreement %.5f" % frac
 
 
 INTEGRATORS = pytest.mark.parametrize("integ", [0, 1, 2, 3, 4], ids=["path", "volpath", "direct", "normal", "depth"])
@@ -135,4 +137,4 @@ def test_other_integrators_paths(gpu_lib, integ, scene):
     g, o = _render_both(gpu_lib, sb, cam, opts, opts.width * opts.height * 4)
     frac, _ = path_agreement(g, o)
     assert np.isfinite(g).all()
-    assert frac >= 0.99, "per-path agreement %.5f" % frac
+    assert frac >= 0.999, "per-path agreement %.5f" % frac
