@@ -62,6 +62,8 @@ def parse():
     p.add_argument("--spp", type=int, default=0)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the batched, adjoint and relMSE records of the default line")
     p.add_argument("--mode", default="auto", choices=["auto", "megakernel", "wavefront", "graph"])
     p.add_argument("--pool", type=int, default=0, help="wavefront path-slot pool size (0 = default)")
     p.add_argument("--block", type=int, default=0, help="trace-kernel block size (0 = default)")
@@ -311,14 +313,12 @@ def workload_scene(args):
     return sb, cam, opts, cfg
 
 
-def main_batched(args):
+def batched_record(steps, warmup):
     """Batched uneven workload: every view of each scene in one lgpu_render_batch call (after
     lgpu_autotune on a 1-spp probe) against the same views rendered one at a time."""
     import torch
     import lambda_gb300 as lg
     from lambda_gb300 import abi, configs
-    lg.build()
-    torch.cuda.set_device(0)
     views = batched_views()
     sbs = [configs.terrain(64, 64, 1, 6)[0], configs.volume(64, 64, 1, 12)[0]]
     rs = [lg.Renderer(sb, device=0) for sb in sbs]
@@ -342,14 +342,14 @@ def main_batched(args):
             rs[sc].render_device(c, o, f.data_ptr())
 
     def timed(fn):
-        for _ in range(max(1, args.warmup)):
+        for _ in range(max(1, warmup)):
             fn()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             fn()
         torch.cuda.synchronize()
-        return (time.perf_counter() - t0) / args.steps
+        return (time.perf_counter() - t0) / steps
 
     for f in films:
         f.zero_()
@@ -357,7 +357,7 @@ def main_batched(args):
     clocks.start()
     tb = timed(batched)
     clk = clocks.stop()
-    counts_ok = all(bool(torch.all(f[..., 3] == float(spp * (max(1, args.warmup) + args.steps))))
+    counts_ok = all(bool(torch.all(f[..., 3] == float(spp * (max(1, warmup) + steps))))
                     for f, (_, _, _, _, spp, _, _) in zip(films, views))
     if not counts_ok:
         raise SystemExit("work check failed: a view's film sample counts do not match its spp")
@@ -365,48 +365,72 @@ def main_batched(args):
     host = [torch.empty_like(f, device="cpu").pin_memory() for f in films]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         batched()
         for h_, f in zip(host, films):
             h_.copy_(f, non_blocking=True)
         torch.cuda.synchronize()
-    te = (time.perf_counter() - t0) / args.steps
-    cfg = {"workload": "batched uneven views: 64 views of the 1080p terrain and the volume/instancing scene, "
-                       "resolution in {128,256,512,1024}^2, spp 1-64, depth 4-12 (seed 6)",
-           "views": len(views), "path_samples": paths, "l2": "scene data and per-view films exceed L2",
-           "tuning": tuning}
-    line = {"metric": METRIC, "value": paths / tb / 1e6, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": tb * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes and views)", "config": cfg,
+    te = (time.perf_counter() - t0) / steps
+    for r in rs:
+        r.close()
+    return {"value": paths / tb / 1e6, "unit": UNIT, "ms_per_step": tb * 1e3,
             "plain": {"value": paths / tp / 1e6, "ms_per_step": tp * 1e3,
                       "scheme": "the same views one at a time through lgpu_render_device (wavefront)"},
             "batched_over_plain": tp / tb,
             "e2e": {"value": paths / te / 1e6, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(sum(f.numel() * 4 for f in films))},
+            "config": {"workload": "batched uneven views: 64 views of the 1080p terrain and the volume/instancing "
+                                   "scene, resolution in {128,256,512,1024}^2, spp 1-64, depth 4-12 (seed 6); one "
+                                   "lgpu_render_batch call per scene", "views": len(views), "path_samples": paths,
+                       "tuning": tuning},
             "clocks": clk}
+
+
+def main_batched(args):
+    import torch
+    import lambda_gb300 as lg
+    lg.build()
+    torch.cuda.set_device(0)
+    rec = batched_record(args.steps, args.warmup)
+    line = {"metric": METRIC, "value": rec["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes and views)",
+            "config": dict(rec["config"], l2="scene data and per-view films exceed L2"),
+            "plain": rec["plain"], "batched_over_plain": rec["batched_over_plain"], "e2e": rec["e2e"],
+            "clocks": rec["clocks"]}
     print(json.dumps(line))
-    for r in rs:
-        r.close()
 
 
-def main_inverse(args):
+def _adam(state, key, x, g, lr, b1=0.9, b2=0.999, eps=1e-8):
+    """One Adam update of parameter x (numpy) with gradient g; state holds the moments."""
+    m, v, t = state.get(key, (np.zeros_like(g), np.zeros_like(g), 0))
+    t += 1
+    m = b1 * m + (1 - b1) * g
+    v = b2 * v + (1 - b2) * g * g
+    state[key] = (m, v, t)
+    mh, vh = m / (1 - b1 ** t), v / (1 - b2 ** t)
+    return x - lr * mh / (np.sqrt(vh) + eps)
+
+
+def inverse_record(steps, warmup):
     """Inverse rendering on the Cornell box at 512^2 with 8 cameras: each step is a 4-spp forward
     render of every camera, the L2 image loss against a seeded ground truth, and the path-replay
-    adjoint of every camera; reports the forward throughput, the backward/forward time ratio and
-    the loss over a few gradient steps on the albedo texture, roughness and sigma_s."""
+    adjoint of every camera (on paths of an independent seed, so the gradient of the loss is
+    unbiased); Adam updates the albedo texture, the GGX roughness and sigma_s.  Reports forward and
+    backward times (bwd/fwd), the loss and the parameter errors over the steps, and the adjoint
+    against common-random-number central differences on a 64^2 frame (texture direction without
+    Russian roulette, and roughness)."""
     import torch
     import lambda_gb300 as lg
     from lambda_gb300 import configs
-    lg.build()
-    torch.cuda.set_device(0)
     Wd = Ht = 512
     spp = 4
     rng = np.random.RandomState(5)
     gt = dict(albedo=rng.uniform(0.1, 0.9, (64, 64, 3)).astype(np.float32), roughness=0.3, sigma_a=0.1, sigma_s=0.8)
     cur = dict(albedo=np.full((64, 64, 3), 0.5, np.float32), roughness=0.6, sigma_a=0.1, sigma_s=0.2)
 
-    def scene(params, seed):
-        sb, cams, opts = configs.cornell_inverse(Wd, Ht, spp, **params)
+    def scene(params, seed, w=Wd, h=Ht, s=spp):
+        sb, cams, opts = configs.cornell_inverse(w, h, s, **params)
         opts.seed = seed
         return lg.Renderer(sb), cams, opts
 
@@ -424,9 +448,10 @@ def main_inverse(args):
     gtex = torch.zeros((64, 64, 4), dtype=torch.float32, device="cuda")
     gsc = torch.zeros(3, dtype=torch.float32, device="cuda")
     dloss = [torch.zeros((Ht, Wd, 4), dtype=torch.float32, device="cuda") for _ in range(8)]
-    fwd_t, bwd_t, losses = [], [], []
-    steps = max(8, args.steps)
-    for it in range(args.warmup + steps):
+    fwd_t, bwd_t, losses, err = [], [], [], []
+    adam = {}
+    n_steps = max(16, steps)
+    for it in range(warmup + n_steps):
         r, cams, opts = scene(cur, 1 + it)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -441,6 +466,9 @@ def main_inverse(args):
             d[..., :3] = 2.0 * diff / npx
         gtex.zero_()
         gsc.zero_()
+        # the adjoint replays paths of an independent seed: with the forward's own paths, the
+        # residual and the derivative would be correlated and d(loss) biased
+        opts.seed = 1_000_003 + it
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         for d, cam in zip(dloss, cams):
@@ -448,28 +476,132 @@ def main_inverse(args):
         torch.cuda.synchronize()
         t3 = time.perf_counter()
         r.close()
-        if it >= args.warmup:
+        if it >= warmup:
             fwd_t.append(t1 - t0)
             bwd_t.append(t3 - t2)
         losses.append(loss)
-        g = gtex.cpu().numpy()[..., :3]
-        s_ = gsc.cpu().numpy()
-        # normalised gradient steps (each parameter group scaled by its gradient's rms)
-        cur["albedo"] = np.clip(cur["albedo"] - 0.05 * g / (np.sqrt(np.mean(g * g)) + 1e-30), 0.02, 0.98).astype(np.float32)
-        cur["roughness"] = float(np.clip(cur["roughness"] - 0.05 * np.sign(s_[0]), 0.05, 1.0))
-        cur["sigma_s"] = float(np.clip(cur["sigma_s"] - 0.1 * np.sign(s_[2]), 0.01, 4.0))
-    paths = 8 * Wd * Ht * spp
+        err.append({"albedo_mae": float(np.mean(np.abs(cur["albedo"] - gt["albedo"]))),
+                    "roughness": cur["roughness"], "sigma_s": cur["sigma_s"]})
+        g = gtex.cpu().numpy()[..., :3].astype(np.float64)
+        s_ = gsc.cpu().numpy().astype(np.float64)
+        cur["albedo"] = np.clip(_adam(adam, "albedo", cur["albedo"], g, 0.03), 0.02, 0.98).astype(np.float32)
+        cur["roughness"] = float(np.clip(_adam(adam, "roughness", np.array(cur["roughness"]), s_[0], 0.03), 0.05, 1.0))
+        cur["sigma_s"] = float(np.clip(_adam(adam, "sigma_s", np.array(cur["sigma_s"]), s_[2], 0.06), 0.01, 4.0))
+    err.append({"albedo_mae": float(np.mean(np.abs(cur["albedo"] - gt["albedo"]))),
+                "roughness": cur["roughness"], "sigma_s": cur["sigma_s"]})
     fwd, bwd = float(np.median(fwd_t)), float(np.median(bwd_t))
-    line = {"metric": METRIC, "value": paths / fwd / 1e6, "unit": UNIT, "n_gpus": 1, "steps": steps,
-            "warmup": args.warmup, "ms_per_step": (fwd + bwd) * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ground-truth texture and parameters)",
+
+    # gradient check: adjoint against CRN central differences on one 64^2 camera
+    w64 = np.random.RandomState(11).uniform(0.0, 1.0, (64, 64, 3))
+    base = dict(albedo=np.random.RandomState(12).uniform(0.1, 0.9, (8, 8, 3)).astype(np.float32),
+                roughness=0.3, sigma_a=0.1, sigma_s=0.8)
+
+    def render64(params, no_rr, s):
+        sb, cams_, o = configs.cornell_inverse(64, 64, s, tex_res=8, **params)
+        if no_rr:
+            o.min_bounces = o.max_bounces
+        rr = lg.Renderer(sb)
+        f = torch.zeros((64, 64, 4), dtype=torch.float32, device="cuda")
+        o.kernel_mode = 2
+        rr.render_device(cams_[3], o, f.data_ptr())
+        torch.cuda.synchronize()
+        fn = f.double().cpu().numpy()
+        val = float(np.sum(fn[..., :3] / fn[..., 3:4] * w64))
+        dl = torch.zeros((64, 64, 4), dtype=torch.float32, device="cuda")
+        dl[..., :3] = torch.from_numpy(w64.astype(np.float32)).cuda()
+        gt_ = torch.zeros((8, 8, 4), dtype=torch.float32, device="cuda")
+        gs_ = torch.zeros(3, dtype=torch.float32, device="cuda")
+        o.kernel_mode = 1
+        rr.adjoint(cams_[3], o, (0, 0, 4, 0), dl.data_ptr(), gt_.data_ptr(), gs_.data_ptr())
+        torch.cuda.synchronize()
+        rr.close()
+        return val, gt_.cpu().numpy()[..., :3].astype(np.float64), gs_.cpu().numpy().astype(np.float64)
+
+    v = np.random.RandomState(3).uniform(-1, 1, (8, 8, 3)).astype(np.float32)
+    _, gtx, _ = render64(base, True, 512)
+    e = 1e-3
+    fp = render64(dict(base, albedo=base["albedo"] + e * v), True, 512)[0]
+    fm = render64(dict(base, albedo=base["albedo"] - e * v), True, 512)[0]
+    fd_tex, adj_tex = (fp - fm) / (2 * e), float(np.sum(gtx * v))
+    _, _, gsr = render64(base, False, 2048)
+    e = 1e-2
+    fp = render64(dict(base, roughness=base["roughness"] + e), False, 2048)[0]
+    fm = render64(dict(base, roughness=base["roughness"] - e), False, 2048)[0]
+    fd_r = (fp - fm) / (2 * e)
+    return {"bwd_fwd_ratio": bwd / fwd, "forward_ms": fwd * 1e3, "backward_ms": bwd * 1e3,
+            "forward_mpath_s": 8 * Wd * Ht * spp / fwd / 1e6,
+            "gradient_check": {"texture_direction": {"adjoint": adj_tex, "finite_difference": fd_tex,
+                                                     "rel_error": abs(adj_tex - fd_tex) / abs(fd_tex),
+                                                     "setup": "64^2, 512 spp, no roulette, eps 1e-3, CRN"},
+                               "roughness": {"adjoint": float(gsr[0]), "finite_difference": fd_r,
+                                             "rel_error": abs(gsr[0] - fd_r) / abs(fd_r),
+                                             "setup": "64^2, 2048 spp, eps 1e-2, CRN"}},
+            "optimisation": {"optimizer": "Adam (lr 0.03 albedo and roughness, 0.06 sigma_s)", "steps": len(losses),
+                             "loss": losses, "params": err,
+                             "truth": {"roughness": gt["roughness"], "sigma_s": gt["sigma_s"]}},
             "config": {"workload": "inverse rendering: Cornell box 512^2, 8 cameras, 4 spp forward + path-replay "
                                    "adjoint, L2 image loss; unknowns 64x64 albedo texture, GGX roughness, medium sigma_s",
-                       "width": Wd, "height": Ht, "spp": spp, "cameras": 8},
-            "forward_ms": fwd * 1e3, "backward_ms": bwd * 1e3, "bwd_fwd_ratio": bwd / fwd,
-            "loss": losses, "final_params": {"roughness": cur["roughness"], "sigma_s": cur["sigma_s"],
-                                             "albedo_mae": float(np.mean(np.abs(cur["albedo"] - gt["albedo"])))}}
+                       "width": Wd, "height": Ht, "spp": spp, "cameras": 8}}
+
+
+def main_inverse(args):
+    import torch
+    import lambda_gb300 as lg
+    lg.build()
+    torch.cuda.set_device(0)
+    rec = inverse_record(args.steps, args.warmup)
+    line = {"metric": METRIC, "value": rec["forward_mpath_s"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": rec["forward_ms"] + rec["backward_ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded ground-truth texture and parameters)", "config": rec["config"],
+            "adjoint": {k: rec[k] for k in ("bwd_fwd_ratio", "forward_ms", "backward_ms", "gradient_check",
+                                             "optimisation")}}
     print(json.dumps(line))
+
+
+def relmse_record(r, cam, opts, stream, rates, threshold=1e-3, ref_spp=4096, ref_seed=777,
+                  levels=(4, 8, 16, 32, 64, 128, 256, 512, 1024)):
+    """Samples per pixel and wall time each renderer needs to reach relMSE <= threshold on this frame.
+
+    Reference image: the GPU render of the same frame at ref_spp with an independent seed.  Test
+    images: the frame at growing spp (progressive passes, seed of opts).  relMSE = mean over pixels and
+    channels of (I - R)^2 / (R^2 + 1e-2).  The GPU and the reference CPU integrator compute the same
+    estimate per path (per-path parity), so they reach the threshold at the same spp and their times
+    to it are spp * pixels / throughput (rates: name -> Mpath-samples/s of this frame; the batched
+    record compares batched and plain on its own views at equal spp)."""
+    import torch
+    W, H = opts.width, opts.height
+    o = type(opts).from_buffer_copy(opts)
+    ref = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    o.seed, o.spp = ref_seed, 256
+    t0 = time.perf_counter()
+    for k in range(ref_spp // 256):
+        o.sample_offset = k * 256
+        r.render_device(cam, o, ref.data_ptr(), stream=stream)
+    torch.cuda.synchronize()
+    t_ref = time.perf_counter() - t0
+    R = (ref[..., :3] / ref[..., 3:4]).double()
+    den = R * R + 1e-2
+    film = torch.zeros_like(ref)
+    o.seed = opts.seed
+    done, curve, hit = 0, [], None
+    for lv in levels:
+        o.spp, o.sample_offset = lv - done, done
+        r.render_device(cam, o, film.data_ptr(), stream=stream)
+        done = lv
+        torch.cuda.synchronize()
+        I = (film[..., :3] / film[..., 3:4]).double()
+        err = float(torch.mean((I - R) ** 2 / den))
+        curve.append([lv, err])
+        if err <= threshold:
+            hit = lv
+            break
+    rec = {"threshold": threshold, "definition": "mean((I - R)^2 / (R^2 + 1e-2)) over pixels and RGB",
+           "reference": "GPU render of the same frame, %d spp, seed %d (%.1f s)" % (ref_spp, ref_seed, t_ref),
+           "curve": curve, "spp_at_threshold": hit}
+    if hit is not None:
+        rec["seconds_to_threshold"] = {k: hit * W * H / (v * 1e6) for k, v in rates.items() if v}
+    return rec
 
 
 def main():
@@ -594,6 +726,15 @@ def main():
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(sb, cam, opts, args.cpu_seconds, gpu=r)
+    extras = {}
+    if not args.no_extras and world == 1 and args.workload == "terrain":
+        # the rest of the metric: batched vs plain, equal-relMSE times, and the adjoint's cost
+        extras["batched"] = batched_record(2, 1)
+        rates = {"gpu_plain": value}
+        if cpu:
+            rates["cpu_" + cpu["kind"]] = cpu["value"]
+        extras["relmse"] = relmse_record(r, cam, opts, stream, rates)
+        extras["adjoint"] = inverse_record(4, 1)
     cfg["l2"] = "scene data > L2 and a 256 MiB buffer is written between timed steps"
     cfg["width"], cfg["height"], cfg["spp"] = W, H, spp
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -602,6 +743,7 @@ def main():
             "config": cfg, "parallelism": "replicas" if world > 1 else "single GPU",
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": W * H * 16, "d2h_bytes_per_step": W * H * 16},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
+    line.update(extras)
     print(json.dumps(line))
     r.close()
     if dist:
