@@ -47,6 +47,7 @@ struct lgpu_context {
     bool tuned = false;         /* lgpu_autotune result, used by kernel_mode AUTO */
     lgpu_tuning tuning;
     unsigned long long *d_counters = nullptr;
+    int *d_err = nullptr;   /* device error word (DeviceScene::err) */
     float4 *d_film = nullptr;
     size_t film_px = 0;
     float4 *d_paths = nullptr;
@@ -73,6 +74,20 @@ struct lgpu_context {
 };
 
 namespace {
+
+int fail(lgpu_context *c, int code, const std::string &msg);
+/* Read (and clear) the device error word after the work of a render has completed on `st`. */
+int check_device_error(lgpu_context *c, cudaStream_t st) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(c, LGPU_ERR_CUDA, std::string("device error word: ") + cudaGetErrorString(e));
+    if (!h) return LGPU_OK;
+    cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
+    cudaStreamSynchronize(st);
+    if (h & 1) return fail(c, LGPU_ERR_QUEUE_OVERFLOW, "BVH traversal stack overflow on the device");
+    return fail(c, LGPU_ERR_TIMEOUT, "path-state copy to shared memory did not complete");
+}
 
 int fail(lgpu_context *c, int code, const std::string &msg) {
     if (c) c->err = msg;
@@ -306,6 +321,8 @@ LGPU_API int lgpu_create(lgpu_context **out, int device) {
     std::memset(&c->S, 0, sizeof(c->S));
     e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     if (e != cudaSuccess) { delete c; return LGPU_ERR_CUDA; }
@@ -318,6 +335,7 @@ LGPU_API void lgpu_destroy(lgpu_context *c) {
     cudaSetDevice(c->device);
     free_scene(c);
     cudaFree(c->d_counters);
+    cudaFree(c->d_err);
     cudaFree(c->d_film);
     cudaFree(c->d_paths);
     cudaFree(c->d_ids);
@@ -865,6 +883,7 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
               upload(c, lightSlot, &S.light_slot, bytes) && upload(c, fpool, &S.fpool, bytes) &&
               upload(c, envTex, &S.env_tex, bytes) && upload(c, media, &S.media, bytes);
     if (!ok) { free_scene(c); return c->err.find("alloc") != std::string::npos ? LGPU_ERR_OOM : LGPU_ERR_CUDA; }
+    S.err = c->d_err;
     c->S = S;
     c->tex_off = H.texOff; c->tex_w = H.texW; c->tex_h = H.texH;
     c->mask_cond = H.maskCond; c->mask_marg = H.maskMarg; c->mask_int = H.maskInt;
@@ -1049,7 +1068,7 @@ int run_graph_loop(lgpu_context *c, WaveArgs &W, bool hero, size_t slots, uint64
     c->stats.pool_slots = (uint32_t)slots;
     c->stats.spawned += n;
     c->stats.launches += launches;
-    return rc;
+    return rc ? rc : check_device_error(c, st);
 }
 
 /* Run the wavefront over `n` paths (chunk indices 0..n-1 = path ids base.. or ids[]), writing
@@ -1186,7 +1205,7 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     c->stats.pool_slots = (uint32_t)slots;
     c->stats.spawned += n;
     c->stats.launches += launches;
-    return LGPU_OK;
+    return check_device_error(c, st);
 }
 
 /* The wavefront state machine is the MIS volumetric integrator; the other integrators run as the
@@ -1295,6 +1314,8 @@ int render_impl(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_
 int finish_timing(lgpu_context *c) {
     cudaError_t e = cudaEventSynchronize(c->ev1);
     if (e != cudaSuccess) return cuda_fail(c, e, "render");
+    const int rc = check_device_error(c, 0);
+    if (rc) return rc;
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->stats.last_render_ms = ms;
@@ -1878,7 +1899,7 @@ LGPU_API int lgpu_render_paths_noalloc(lgpu_context *c, const lgpu_camera_desc *
     c->stats.launches = launches;
     c->stats.iterations = (uint32_t)iters;
     c->stats.pool_slots = (uint32_t)slots;
-    return LGPU_OK;
+    return check_device_error(c, st);
 }
 
 }  // extern "C"

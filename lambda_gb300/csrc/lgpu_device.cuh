@@ -859,7 +859,10 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
                 }
             }
         }
-        if (sp >= LGPU_STACK - 2) sp = LGPU_STACK - 2;   /* never reached for BVH depths < 60 */
+        if (sp >= LGPU_STACK - 2) {   /* depth is checked at commit; report instead of dropping nodes */
+            atomicOr(S.err, 1);
+            return hit;
+        }
     }
     return hit;
 }

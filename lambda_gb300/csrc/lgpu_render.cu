@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <atomic>
 
+#include "lgpu_bulk.cuh"
 #include "lgpu_camera.cuh"
 #include "lgpu_integrator.cuh"
 #include "lgpu_launch.h"
@@ -275,23 +276,71 @@ __device__ __forceinline__ void warp_stage(PHot<NS> *G, PHot<NS> *sh, int slot, 
     __syncwarp();
 }
 
+/* Bulk staging: every lane copies its own slot's record with one cp.async.bulk; the warp's copies
+ * complete on the warp's mbarrier, so the warp waits one memory round trip for all 32 records.
+ * Returns false (and sets the device error bit) if the bounded wait ran out; the caller then stops. */
+template <int NS>
+__device__ __forceinline__ bool bulk_stage_in(const PHot<NS> *G, PHot<NS> *sh, int slot, uint64_t *bar, uint32_t &phase,
+                                              int *err) {
+    const unsigned act = __ballot_sync(0xffffffffu, slot >= 0);
+    if (!act) return true;
+    const int lane = threadIdx.x & 31;
+    bulk_wait_read();            /* this lane's last store has read its record */
+    fence_proxy_async_smem();    /* and its ordinary accesses to the record come before the copy */
+    __syncwarp();
+    if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)__popc(act) * (uint32_t)sizeof(PHot<NS>));
+    __syncwarp();
+    if (slot >= 0) bulk_load(sh + lane, G + slot, (uint32_t)sizeof(PHot<NS>), bar);
+    const bool ok = mbar_wait(bar, phase);
+    phase ^= 1u;
+    if (!ok) atomicOr(err, LG_ERR_STAGE_TIMEOUT);
+    return __all_sync(0xffffffffu, ok);
+}
+/* the lane's updated record back to its slot (no-op for keep < 0) */
+template <int NS>
+__device__ __forceinline__ void bulk_stage_out(PHot<NS> *G, PHot<NS> *sh, int keep) {
+    if (keep < 0) return;
+    fence_proxy_async_smem();    /* the thread's writes to its record, before the copy engine reads it */
+    bulk_store(G + keep, sh + (threadIdx.x & 31), (uint32_t)sizeof(PHot<NS>));
+    bulk_commit();
+}
+/* one mbarrier per warp, after the block's records in dynamic shared memory */
+template <int NS>
+__device__ __forceinline__ uint64_t *warp_barrier(float4 *smem) {
+    uint64_t *bar = reinterpret_cast<uint64_t *>(reinterpret_cast<PHot<NS> *>(smem) + blockDim.x) + (threadIdx.x >> 5);
+    if ((threadIdx.x & 31) == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    return bar;
+}
+
 /* Continue every slot of the (segmented) input queue until its next query or its end.  Grid-stride:
  * a launch sized to the queue runs the loop body once per thread; a device-driven launch (fixed
  * grid, n read from W.count_in) loops.  The loop bound is block-uniform, so warps stay converged
- * for the warp-cooperative staging. */
+ * for the warp-wide staging. */
 /* Build-time tuning knobs (defaults are the measured best on the 1080p terrain):
  * LGPU_RESUME_MINB: minimum resident blocks per SM requested from the compiler for resume/spawn;
- * LGPU_NO_STAGE: path states are used in place in HBM instead of staged through shared memory. */
+ * LGPU_NO_STAGE: path states are used in place in HBM instead of staged through shared memory;
+ * LGPU_WARP_STAGE: staging by warp-cooperative coalesced copies instead of bulk copies. */
 #ifndef LGPU_RESUME_MINB
 #define LGPU_RESUME_BOUNDS __launch_bounds__(128)
 #else
 #define LGPU_RESUME_BOUNDS __launch_bounds__(128, LGPU_RESUME_MINB)
 #endif
-#ifdef LGPU_NO_STAGE
-#define LG_STAGE(G, sh, slot, in)
+#if defined(LGPU_NO_STAGE)
+#define LG_STAGE_IN(G, sh, slot) true
+#define LG_STAGE_OUT(G, sh, keep)
 #define LG_STATE(G, sh, slot) (G[slot])
+#elif defined(LGPU_WARP_STAGE)
+#define LG_STAGE_IN(G, sh, slot) (warp_stage<NS>(G, sh, slot, true), true)
+#define LG_STAGE_OUT(G, sh, keep) warp_stage<NS>(G, sh, keep, false)
+#define LG_STATE(G, sh, slot) (sh[threadIdx.x & 31])
 #else
-#define LG_STAGE(G, sh, slot, in) warp_stage<NS>(G, sh, slot, in)
+#define LG_BULK_STAGE 1
+#define LG_STAGE_IN(G, sh, slot) bulk_stage_in<NS>(G, sh, slot, bar, phase, W.S.err)
+#define LG_STAGE_OUT(G, sh, keep) bulk_stage_out<NS>(G, sh, keep)
 #define LG_STATE(G, sh, slot) (sh[threadIdx.x & 31])
 #endif
 
@@ -301,6 +350,10 @@ __global__ void LGPU_RESUME_BOUNDS k_wave_resume(const __grid_constant__ WaveArg
     if (DEV) n = W.count_in[W.seg_sel];
     PHot<NS> *G = reinterpret_cast<PHot<NS> *>(W.states);
     PHot<NS> *sh = reinterpret_cast<PHot<NS> *>(smem4) + (threadIdx.x & ~31);
+#ifdef LG_BULK_STAGE
+    uint64_t *bar = warp_barrier<NS>(smem4);
+    uint32_t phase = 0;
+#endif
     const int step = DEV ? gridDim.x * blockDim.x : n;   /* host-sized launches run the body once */
     for (int base = blockIdx.x * blockDim.x; base < n; base += step) {
         const int i = base + threadIdx.x;
@@ -315,7 +368,7 @@ __global__ void LGPU_RESUME_BOUNDS k_wave_resume(const __grid_constant__ WaveArg
                 slot = W.queue_in[seg * W.cap_in + (i - W.seg_off[seg])];
             }
         }
-        LG_STAGE(G, sh, slot, true);
+        if (!LG_STAGE_IN(G, sh, slot)) break;
         int keep = -1;
         if (slot >= 0) {
             PHot<NS> &s = LG_STATE(G, sh, slot);
@@ -330,8 +383,11 @@ __global__ void LGPU_RESUME_BOUNDS k_wave_resume(const __grid_constant__ WaveArg
             else { wave_save(w, s); keep = slot; }
         }
         __syncwarp();
-        LG_STAGE(G, sh, keep, false);
+        LG_STAGE_OUT(G, sh, keep);
     }
+#ifdef LG_BULK_STAGE
+    bulk_wait_all();
+#endif
 }
 
 /* Start new paths in free slots: consecutive path ids go to consecutive free-list entries, so the
@@ -361,8 +417,14 @@ __global__ void LGPU_RESUME_BOUNDS k_wave_spawn(const __grid_constant__ WaveArgs
             else { wave_save(w, s); keep = slot; }
         }
         __syncwarp();
-        LG_STAGE(G, sh, keep, false);
+        LG_STAGE_OUT(G, sh, keep);
+#ifdef LG_BULK_STAGE
+        bulk_wait_read();   /* the record is rebuilt in place by the next iteration */
+#endif
     }
+#ifdef LG_BULK_STAGE
+    bulk_wait_all();
+#endif
 }
 /* next_path += paths started by the last spawn; clear the free list. */
 static __global__ void k_wave_advance(WaveArgs W, int n_max, int fresh) {
@@ -376,10 +438,12 @@ static __global__ void k_wave_advance(WaveArgs W, int n_max, int fresh) {
 
 cudaError_t LG_CAT(wave_resume_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, int start_new, cudaStream_t st) {
     constexpr bool C = LGPU_COUNT != 0;
-#ifdef LGPU_NO_STAGE
+#if defined(LGPU_NO_STAGE)
     const size_t smem = 0;
-#else
+#elif defined(LGPU_WARP_STAGE)
     const size_t smem = 128 * sizeof(PHot<LGPU_NS>);
+#else
+    const size_t smem = 128 * sizeof(PHot<LGPU_NS>) + (128 / 32) * sizeof(uint64_t);   /* records + warp barriers */
 #endif
     static std::atomic<int> grids_resume[LG_MAX_DEVICES], grids_spawn[LG_MAX_DEVICES];
     const int dev = current_device();

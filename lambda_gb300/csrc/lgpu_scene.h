@@ -179,4 +179,6 @@ struct DeviceScene {
     float tree_power, inf_power;
     int env_light;               /* light index of the environment light or -1 */
     int has_volumes;
+    int *err;                    /* device error word of the context (bits: traversal stack overflow,
+                                  * path-state staging wait ran out), read and cleared by the host */
 };

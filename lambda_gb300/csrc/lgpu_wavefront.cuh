@@ -95,6 +95,9 @@ struct __align__(16) PCold {
     float3 trO, trD;
 };
 
+/* bulk copies move whole records: sizes must be multiples of 16 bytes */
+static_assert(sizeof(PHot<3>) % 16 == 0 && sizeof(PHot<4>) % 16 == 0, "path-state record not 16-byte sized");
+
 struct WaveArgs {
     DeviceScene S;
     CamParams cam;
