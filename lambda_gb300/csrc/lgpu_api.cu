@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -143,7 +144,9 @@ struct HostScene {
     std::vector<int> texOff, texW, texH;   /* image textures in the texel pool */
     std::vector<int> maskCond, maskMarg;   /* per texture: masked-aperture Piecewise2D offsets in fpool (-1: none) */
     std::vector<float> maskInt;
-    std::vector<DNode> nodes;
+    std::vector<BvhNode> nodes;
+    int bvh_depth = 0;                     /* node levels of the deepest TLAS + BLAS descent */
+    mutable int bvh_stack = 0;             /* worst-case traversal stack entries (set by validate_scene) */
     std::vector<DTri> tris;
     std::vector<DInst> insts;
     std::vector<DObject> objects;
@@ -173,28 +176,51 @@ bool check_ref(const HostScene &H, int ref, bool tlas, std::string &why) {
     return true;
 }
 
-/* Walk every BVH (TLAS and each BLAS) from its root; check refs, depth and leaf ranges. */
-bool check_bvh(const HostScene &H, int root, bool tlas, std::string &why) {
-    std::vector<std::pair<int, int>> st;   /* (ref, depth) */
+/* Walk a BVH (the TLAS, or a BLAS) from its root and check refs and leaf ranges.  `need` receives
+ * the most traversal-stack entries a ray can hold in it, counted the way traverse_t pushes: each
+ * entry carries the entries left below it once it is popped (0 for the root), an inner node
+ * pushes up to all its children, a TLAS leaf pushes the instance marker and the BLAS root.  BLAS
+ * results are memoised by root since instances share them. */
+bool check_bvh(const HostScene &H, int root, bool tlas, std::string &why, int &need,
+               std::map<int, int> &blas_need) {
+    std::vector<std::pair<int, int>> st;   /* (ref, entries below it once popped) */
     st.push_back({root, 0});
+    need = 1;
     size_t visits = 0;
     while (!st.empty()) {
         auto e = st.back();
         st.pop_back();
-        if (++visits > 4 * (H.nodes.size() + H.tris.size() + H.insts.size() + 4)) { why = "BVH has a cycle"; return false; }
+        if (++visits > 16 * (H.nodes.size() + H.tris.size() + H.insts.size() + 4)) { why = "BVH has a cycle"; return false; }
         if (!check_ref(H, e.first, tlas, why)) return false;
-        if (e.second > LGPU_STACK - 8) { why = "BVH deeper than the traversal stack"; return false; }
+        if (e.second > LGPU_STACK) { why = "BVH deeper than the traversal stack"; return false; }
         const int idx = e.first >> 4, cnt = e.first & 15;
         if (cnt == 0) {
-            const DNode &n = H.nodes[idx];
-            st.push_back({n.ch.x, e.second + 1});
-            st.push_back({n.ch.y, e.second + 1});
-        } else if (tlas) {
-            for (int k = 0; k < cnt; ++k) {
-                const DInst &I = H.insts[idx + k];
-                if (I.object >= (int)H.objects.size()) { why = "instance object out of range"; return false; }
-                if (!check_bvh(H, I.root, false, why)) return false;
+            int ch[8], nch = 0;
+#if LGPU_BVH_WIDE
+            const DWide &n = H.nodes[idx];
+            if (n.nchild > 8) { why = "wide node with more than eight children"; return false; }
+            for (int k = 0; k < n.nchild; ++k) {
+                const int m = n.meta[k], c = m & 7, off = m >> 3;
+                ch[nch++] = c ? (((n.leaf_base + off) << 4) | c) : ((n.child_base + off) << 4);
             }
+#else
+            const DNode &n = H.nodes[idx];
+            ch[nch++] = n.ch.x;
+            ch[nch++] = n.ch.y;
+#endif
+            need = std::max(need, e.second + nch);
+            for (int k = 0; k < nch; ++k) st.push_back({ch[k], e.second + nch - 1});
+        } else if (tlas) {
+            if (cnt != 1) { why = "TLAS leaf with more than one instance"; return false; }
+            const DInst &I = H.insts[idx];
+            if (I.object >= (int)H.objects.size()) { why = "instance object out of range"; return false; }
+            auto it = blas_need.find(I.root);
+            if (it == blas_need.end()) {
+                int bn = 0;
+                if (!check_bvh(H, I.root, false, why, bn, blas_need)) return false;
+                it = blas_need.emplace(I.root, bn).first;
+            }
+            need = std::max(need, std::max(e.second + 2, e.second + 1 + it->second));
         } else {
             for (int k = 0; k < cnt; ++k) {
                 const DTri &T = H.tris[idx + k];
@@ -226,7 +252,12 @@ bool check_prog(const HostScene &H, int off, int len, std::string &why) {
 
 bool validate_scene(const HostScene &H, std::string &why) {
     const DeviceScene &S = H.S;
-    if (!check_bvh(H, S.root, S.use_tlas != 0, why)) return false;
+    std::map<int, int> blas_need;
+    if (!check_bvh(H, S.root, S.use_tlas != 0, why, H.bvh_stack, blas_need)) return false;
+    if (H.bvh_stack > LGPU_STACK) {
+        why = "BVH needs " + std::to_string(H.bvh_stack) + " traversal-stack entries, the device holds " + std::to_string(LGPU_STACK);
+        return false;
+    }
     const size_t fp = H.fpool.size();
     for (size_t t = 0; t < H.maskCond.size(); ++t) {   /* masked-aperture distributions */
         if (H.maskCond[t] < 0) continue;
@@ -362,7 +393,9 @@ LGPU_API int lgpu_scene_check(const lgpu_scene_desc *d, char *report, size_t rep
         std::string why;
         if (!validate_scene(H, why)) { rc = LGPU_ERR_INVALID_SCENE; msg = "validation: " + why; }
         else {
-            msg = "ok nodes=" + std::to_string(H.nodes.size()) + " tris=" + std::to_string(H.tris.size()) +
+            msg = "ok nodes=" + std::to_string(H.nodes.size()) + " depth=" + std::to_string(H.bvh_depth) +
+                  " stack=" + std::to_string(H.bvh_stack) +
+                  " tris=" + std::to_string(H.tris.size()) +
                   " insts=" + std::to_string(H.insts.size()) + " prog=" + std::to_string(H.code.size()) +
                   " lnodes=" + std::to_string(H.lnodes.size()) + " fpool=" + std::to_string(H.fpool.size()) +
                   " tree_power=" + std::to_string(H.S.tree_power);
@@ -470,7 +503,7 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
     }
 
     /* ---------------- geometry: BLAS / TLAS */
-    std::vector<DNode> &nodes = H.nodes;
+    std::vector<BvhNode> &nodes = H.nodes;
     std::vector<DTri> &tris = H.tris;
     std::vector<DInst> &insts = H.insts;
     auto make_tri = [&](const lgpu_mesh_desc &m, uint32_t t, int objId) {
@@ -503,9 +536,9 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
     {
         std::vector<Aabb> boxes(worldPrims.size());
         for (size_t k = 0; k < worldPrims.size(); ++k) boxes[k] = tri_box(d->meshes[d->objects[worldPrims[k].first].mesh], worldPrims[k].second);
-        BvhOut bo;
-        build_bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo);
-        maxDepth = std::max(maxDepth, bo.max_depth);
+        DeviceBvh bo;
+        build_device_bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo);
+        maxDepth = std::max(maxDepth, bo.depth);
         nodes.insert(nodes.end(), bo.nodes.begin(), bo.nodes.end());
         for (uint32_t k : bo.order) {
             const auto &wp = worldPrims[k];
@@ -538,9 +571,9 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
                 const lgpu_mesh_desc &m = d->meshes[o.mesh];
                 std::vector<Aabb> boxes(m.num_triangles);
                 for (uint32_t t = 0; t < m.num_triangles; ++t) boxes[t] = tri_box(m, t);
-                BvhOut bo;
-                build_bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo);
-                maxDepth = std::max(maxDepth, bo.max_depth);
+                DeviceBvh bo;
+                build_device_bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo);
+                maxDepth = std::max(maxDepth, bo.depth);
                 nodes.insert(nodes.end(), bo.nodes.begin(), bo.nodes.end());
                 for (uint32_t k : bo.order) tris.push_back(make_tri(m, k, -1));
                 blasRoot[o.mesh] = bo.root_ref;
@@ -561,20 +594,20 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
             ab.hi[0] = b.mx.x; ab.hi[1] = b.mx.y; ab.hi[2] = b.mx.z;
             instBoxes.push_back(ab);
         }
-        BvhOut bo;
-        build_bvh(instBoxes, 1, (int)nodes.size(), 0, bo);
+        DeviceBvh bo;
+        build_device_bvh(instBoxes, 1, (int)nodes.size(), 0, bo);
         nodes.insert(nodes.end(), bo.nodes.begin(), bo.nodes.end());
         std::vector<DInst> reordered;
         for (uint32_t k : bo.order) reordered.push_back(insts[k]);
         insts.swap(reordered);
         S.root = bo.root_ref;
         S.use_tlas = 1;
-        maxDepth += bo.max_depth + 1;
+        maxDepth += bo.depth;
     } else {
         S.root = worldRoot;
         S.use_tlas = 0;
     }
-    if (maxDepth > LGPU_STACK - 4) return fail(c, LGPU_ERR_INVALID_SCENE, "BVH too deep for the traversal stack");
+    H.bvh_depth = maxDepth;   /* the stack bound is checked by validate_scene */
 
     /* ---------------- materials */
     std::vector<DIns> &code = H.code;
@@ -891,9 +924,9 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
     c->num_materials = (int)H.mats.size();
     c->have_scene = true;
     c->stats.bvh_nodes = nodes.size();
-    c->stats.bvh_bytes = nodes.size() * sizeof(DNode);
+    c->stats.bvh_bytes = nodes.size() * sizeof(BvhNode);
     c->stats.tri_bytes = tris.size() * sizeof(DTri);
-    c->stats.node_bytes = sizeof(DNode);
+    c->stats.node_bytes = sizeof(BvhNode);
     c->stats.tri_record_bytes = sizeof(DTri);
     c->stats.device_bytes = bytes;
     return LGPU_OK;

@@ -25,6 +25,43 @@ struct BvhOut {
 };
 void build_bvh(const std::vector<Aabb> &boxes, int max_leaf, int node_base, int prim_base, BvhOut &out);
 
+/* The BVH2 collapsed into 8-wide nodes (each node takes its two children, then repeatedly opens
+ * the inner child of largest surface area until it holds eight or only leaves), child boxes
+ * quantised outwards to 8 bits.  Node records are numbered from node_base, primitive order from
+ * prim_base: `order` lists the primitives so that each node's leaf primitives are consecutive.
+ * root_ref encodes the root like a child ref; depth is the number of node levels.  stack is the
+ * most entries a traversal of this tree alone can hold: the maximum over nodes of the node's child
+ * count plus (children - 1) summed over its ancestors (a traversal starts with the root pushed,
+ * each popped node pushes at most all its children, a popped leaf pushes nothing). */
+struct WideOut {
+    std::vector<DWide> nodes;
+    std::vector<uint32_t> order;
+    int root_ref = 0;
+    int depth = 0;
+    int stack = 1;
+};
+void build_wide(const std::vector<Aabb> &boxes, int max_leaf, int node_base, int prim_base, WideOut &out);
+
+/* The device BVH of the compiled layout (LGPU_BVH_WIDE): nodes, primitive order, root ref and
+ * node-level depth. */
+struct DeviceBvh {
+    std::vector<BvhNode> nodes;
+    std::vector<uint32_t> order;
+    int root_ref = 0;
+    int depth = 0;
+};
+inline void build_device_bvh(const std::vector<Aabb> &boxes, int max_leaf, int node_base, int prim_base, DeviceBvh &out) {
+#if LGPU_BVH_WIDE
+    WideOut w;
+    build_wide(boxes, max_leaf, node_base, prim_base, w);
+    out.nodes.swap(w.nodes); out.order.swap(w.order); out.root_ref = w.root_ref; out.depth = w.depth;
+#else
+    BvhOut b;
+    build_bvh(boxes, max_leaf, node_base, prim_base, b);
+    out.nodes.swap(b.nodes); out.order.swap(b.order); out.root_ref = b.root_ref; out.depth = b.max_depth;
+#endif
+}
+
 /* Shader-graph compiler: DAG -> linear bytecode with one register per live value. */
 struct GraphCompiler {
     const lgpu_scene_desc *d = nullptr;

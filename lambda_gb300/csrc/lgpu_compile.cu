@@ -12,6 +12,7 @@
  * allocator maps the SSA values onto LGPU_MAX_REGS float4 registers.
  */
 #include <algorithm>
+#include <deque>
 #include <cmath>
 #include <cstring>
 #include <functional>
@@ -169,6 +170,147 @@ void build_bvh(const std::vector<Aabb> &boxes, int max_leaf, int node_base, int 
         stack.push_back({nodeIdx, 1, mid, j.first + j.count - mid, j.depth + 1});
         stack.push_back({nodeIdx, 0, j.first, mid - j.first, j.depth + 1});
     }
+}
+
+/* ------------------------------------------------------------------ 8-wide collapse */
+namespace {
+
+struct WideCand {
+    Aabb box;
+    int ref;
+};
+
+/* decoded plane p + q * s (q * s exact): the expression the traversal evaluates */
+inline float wide_plane(float p, int q, float s) {
+    const float qs = (float)q * s;
+    return p + qs;
+}
+inline float wide_scale(int e) {   /* 2^(e - 127), e in 1..254 */
+    uint32_t b = (uint32_t)e << 23;
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+/* Quantisation frame of a node box and the outward-rounded 8-bit planes of its children. */
+void quantise(DWide &w, const Aabb &node, const std::vector<WideCand> &ch) {
+    const float p[3] = {node.lo[0], node.lo[1], node.lo[2]};
+    w.px = p[0]; w.py = p[1]; w.pz = p[2];
+    int e[3];
+    for (int a = 0; a < 3; ++a) {
+        const float ext = node.hi[a] - node.lo[a];
+        int ee = 1;
+        if (ext > 0.f && std::isfinite(ext)) {
+            int x2;
+            std::frexp(ext / 255.f, &x2);   /* ext / 255 < 2^x2 */
+            ee = std::min(std::max(x2 + 127, 1), 254);
+        }
+        while (ee < 254 && wide_plane(p[a], 255, wide_scale(ee)) < node.hi[a]) ++ee;
+        e[a] = ee;
+    }
+    w.ex = (uint8_t)e[0]; w.ey = (uint8_t)e[1]; w.ez = (uint8_t)e[2];
+    for (size_t k = 0; k < ch.size(); ++k) {
+        for (int a = 0; a < 3; ++a) {
+            const float s = wide_scale(e[a]);
+            int lo = (int)std::floor((ch[k].box.lo[a] - p[a]) / s);
+            int hi = (int)std::ceil((ch[k].box.hi[a] - p[a]) / s);
+            lo = std::min(std::max(lo, 0), 255);
+            hi = std::min(std::max(hi, 0), 255);
+            while (lo > 0 && wide_plane(p[a], lo, s) > ch[k].box.lo[a]) --lo;
+            while (hi < 255 && wide_plane(p[a], hi, s) < ch[k].box.hi[a]) ++hi;
+            w.qlo[a][k] = (uint8_t)lo;
+            w.qhi[a][k] = (uint8_t)hi;
+        }
+    }
+}
+
+}  // namespace
+
+void build_wide(const std::vector<Aabb> &boxes, int max_leaf, int node_base, int prim_base, WideOut &out) {
+    BvhOut b2;
+    build_bvh(boxes, max_leaf, 0, 0, b2);
+    out.nodes.clear();
+    out.order.clear();
+    out.depth = 0;
+    out.stack = 1;
+    DWide empty;
+    std::memset(&empty, 0, sizeof(empty));
+    empty.ex = empty.ey = empty.ez = 127;
+    if (boxes.empty()) {   /* no primitives: one node without children */
+        out.nodes.push_back(empty);
+        out.root_ref = node_base << 4;
+        return;
+    }
+    if (b2.root_ref & 15) {   /* the whole set is one leaf */
+        out.order = b2.order;
+        out.nodes.push_back(empty);   /* unused placeholder keeps node numbering simple */
+        out.root_ref = (prim_base << 4) | (b2.root_ref & 15);
+        return;
+    }
+    auto children = [&](int idx, std::vector<WideCand> &v) {
+        const DNode &d = b2.nodes[idx];
+        WideCand a, b;
+        a.box.lo[0] = d.xs.x; a.box.hi[0] = d.xs.y; a.box.lo[1] = d.ys.x; a.box.hi[1] = d.ys.y;
+        a.box.lo[2] = d.zs.x; a.box.hi[2] = d.zs.y; a.ref = d.ch.x;
+        b.box.lo[0] = d.xs.z; b.box.hi[0] = d.xs.w; b.box.lo[1] = d.ys.z; b.box.hi[1] = d.ys.w;
+        b.box.lo[2] = d.zs.z; b.box.hi[2] = d.zs.w; b.ref = d.ch.y;
+        v.push_back(a);
+        v.push_back(b);
+    };
+    /* anc = entries a traversal can hold below this node's pushes: the sum of (children - 1) over
+     * its ancestors */
+    struct Item { int ref; Aabb box; int wide, depth, anc; };
+    std::deque<Item> queue;
+    {
+        std::vector<WideCand> r;
+        children(b2.root_ref >> 4, r);
+        Aabb rb = r[0].box;
+        grow(rb, r[1].box);
+        queue.push_back({b2.root_ref, rb, 0, 1, 0});
+    }
+    out.nodes.push_back(empty);
+    std::vector<WideCand> ch;
+    while (!queue.empty()) {
+        const Item it = queue.front();
+        queue.pop_front();
+        out.depth = std::max(out.depth, it.depth);
+        ch.clear();
+        children(it.ref >> 4, ch);
+        while (ch.size() < 8) {   /* open the inner child of largest surface area */
+            int best = -1;
+            float ba = -1.f;
+            for (size_t i = 0; i < ch.size(); ++i)
+                if ((ch[i].ref & 15) == 0 && area(ch[i].box) > ba) { ba = area(ch[i].box); best = (int)i; }
+            if (best < 0) break;
+            std::vector<WideCand> sub;
+            children(ch[best].ref >> 4, sub);
+            ch[best] = sub[0];
+            ch.insert(ch.begin() + best + 1, sub[1]);
+        }
+        DWide w = empty;
+        w.nchild = (uint8_t)ch.size();
+        out.stack = std::max(out.stack, it.anc + (int)ch.size());
+        quantise(w, it.box, ch);
+        const int base = (int)out.nodes.size();
+        const int leaf0 = (int)out.order.size();
+        w.child_base = node_base + base;
+        w.leaf_base = prim_base + leaf0;
+        int inner = 0;
+        for (size_t k = 0; k < ch.size(); ++k) {
+            if ((ch[k].ref & 15) == 0) {
+                w.meta[k] = (uint8_t)(inner << 3);
+                queue.push_back({ch[k].ref, ch[k].box, base + inner, it.depth + 1, it.anc + (int)ch.size() - 1});
+                ++inner;
+            } else {
+                const int first = ch[k].ref >> 4, cnt = ch[k].ref & 15;
+                w.meta[k] = (uint8_t)(((int)out.order.size() - leaf0) << 3 | cnt);
+                for (int j = 0; j < cnt; ++j) out.order.push_back(b2.order[first + j]);
+            }
+        }
+        for (int i = 0; i < inner; ++i) out.nodes.push_back(empty);
+        out.nodes[it.wide] = w;
+    }
+    out.root_ref = node_base << 4;
 }
 
 /* ------------------------------------------------------------------ shader-graph compiler */

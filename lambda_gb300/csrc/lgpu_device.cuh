@@ -784,12 +784,56 @@ struct SmemStack {
     __device__ __forceinline__ int &operator[](int i) { return p[i * LG_SMEM_STRIDE]; }
 };
 
-/* Closest hit (any_hit = false) or occlusion (any_hit = true) over TLAS + BLAS. */
+#if LGPU_BVH_WIDE
+/* One 8-wide node against a ray: keys[k] = (entry distance bits with the low 3 bits replaced by
+ * k) for each child box the ray enters before `best`, sorted ascending; ~0u for the others.
+ * Slab distances take one multiply-add per plane, t = q * (s * inv) + (p - o) * inv, with the near
+ * and far planes of each axis chosen by the sign of the direction once per node.  A plane byte q
+ * becomes a float without the conversion pipe: a byte permute writes it into the low mantissa of
+ * 2^23 (0x4B0000qq) and subtracting 2^23 leaves q exactly. */
+__device__ __forceinline__ void wide_keys(const float4 h0, const int4 qa, const int4 qb, const int4 qc, float3 o,
+                                          float3 inv, float best, uint32_t key[8]) {
+    const uint32_t eb = __float_as_uint(h0.w);
+    const int nch = (int)(eb >> 24);
+    const float ax = __fmul_rn(__fsub_rn(h0.x, o.x), inv.x), ay = __fmul_rn(__fsub_rn(h0.y, o.y), inv.y);
+    const float az = __fmul_rn(__fsub_rn(h0.z, o.z), inv.z);
+    const float bx = __fmul_rn(__uint_as_float((eb & 0xffu) << 23), inv.x);
+    const float by = __fmul_rn(__uint_as_float(((eb >> 8) & 0xffu) << 23), inv.y);
+    const float bz = __fmul_rn(__uint_as_float(((eb >> 16) & 0xffu) << 23), inv.z);
+    /* byte words: qa = lo x (children 0-3, 4-7), lo y; qb = lo z, hi x; qc = hi y, hi z */
+    const bool sx = inv.x < 0.f, sy = inv.y < 0.f, sz = inv.z < 0.f;
+    const uint32_t nx0 = sx ? qb.z : qa.x, nx1 = sx ? qb.w : qa.y, fx0 = sx ? qa.x : qb.z, fx1 = sx ? qa.y : qb.w;
+    const uint32_t ny0 = sy ? qc.x : qa.z, ny1 = sy ? qc.y : qa.w, fy0 = sy ? qa.z : qc.x, fy1 = sy ? qa.w : qc.y;
+    const uint32_t nz0 = sz ? qc.z : qb.x, nz1 = sz ? qc.w : qb.y, fz0 = sz ? qb.x : qc.z, fz1 = sz ? qb.y : qc.w;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+#define LG_QF(w0, w1) __fsub_rn(__uint_as_float(__byte_perm((k < 4 ? (w0) : (w1)), 0x4B000000u, 0x7440u | (uint32_t)(k & 3))), 8388608.f)
+        const float tnx = __fmaf_rn(LG_QF(nx0, nx1), bx, ax), tfx = __fmaf_rn(LG_QF(fx0, fx1), bx, ax);
+        const float tny = __fmaf_rn(LG_QF(ny0, ny1), by, ay), tfy = __fmaf_rn(LG_QF(fy0, fy1), by, ay);
+        const float tnz = __fmaf_rn(LG_QF(nz0, nz1), bz, az), tfz = __fmaf_rn(LG_QF(fz0, fz1), bz, az);
+#undef LG_QF
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, best));
+        key[k] = (k < nch && tn <= tf) ? ((__float_as_uint(tn) & ~7u) | (uint32_t)k) : 0xffffffffu;
+    }
+    /* Batcher's odd-even merge network for eight keys (19 compare-exchanges) */
+#define LG_CX(i, j) { const uint32_t lo = umin(key[i], key[j]); key[j] = umax(key[i], key[j]); key[i] = lo; }
+    LG_CX(0, 1) LG_CX(2, 3) LG_CX(4, 5) LG_CX(6, 7) LG_CX(0, 2) LG_CX(1, 3) LG_CX(4, 6) LG_CX(5, 7) LG_CX(1, 2)
+    LG_CX(5, 6) LG_CX(0, 4) LG_CX(3, 7) LG_CX(1, 5) LG_CX(2, 6) LG_CX(1, 4) LG_CX(3, 6) LG_CX(2, 4) LG_CX(3, 5)
+    LG_CX(3, 4)
+#undef LG_CX
+}
+#endif
+
+/* Closest hit (any_hit = false) or occlusion (any_hit = true) over TLAS + BLAS.  The entry being
+ * visited is held in `e`; a node continues with its nearest hit child and pushes the others far to
+ * near, so the next nearest is popped first.  Every push is checked against the stack: the host
+ * refuses scenes whose worst case exceeds it, so the check only reports a broken bound. */
 template <bool COUNT, class STK>
 __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, float3 wd, float tmax, bool any_hit, HitRec *hr,
                                            TravStats *st, STK &stack) {
     int sp = 0;
-    stack[sp++] = S.root;   /* encoded child ref of the root */
+    int e = S.root;   /* encoded child ref of the root */
     float3 o = wo, d = wd;
     float3 inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
     float best = tmax;
@@ -797,15 +841,17 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
     bool hit = false;
     bool in_blas = !S.use_tlas;
     if (COUNT) st->rays++;
-    while (sp > 0) {
-        const int e = stack[--sp];
+    while (true) {
         if (e == LG_MARKER) {
             o = wo; d = wd; inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
             in_blas = false; inst_obj = -1;
+            if (sp == 0) break;
+            e = stack[--sp];
             continue;
         }
         const int ref = e >> LG_LEAF_BITS, cnt = e & ((1 << LG_LEAF_BITS) - 1);
         if (cnt == 0) {
+#if !LGPU_BVH_WIDE
             const DNode *n = S.nodes + ref;
             const float4 xs = ldg4(&n->xs), ys = ldg4(&n->ys), zs = ldg4(&n->zs);
             const int4 ch = ldg4i(&n->ch);
@@ -821,11 +867,52 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
             const float bn = fmaxf(fmaxf(fminf(bx0, bx1), fminf(by0, by1)), fmaxf(fminf(bz0, bz1), 0.f));
             const float bf = fminf(fminf(fmaxf(bx0, bx1), fmaxf(by0, by1)), fminf(fmaxf(bz0, bz1), best));
             const bool ha = an <= af, hb = bn <= bf;
-            if (ha && hb) {
-                if (an <= bn) { stack[sp++] = ch.y; stack[sp++] = ch.x; }
-                else { stack[sp++] = ch.x; stack[sp++] = ch.y; }
-            } else if (ha) stack[sp++] = ch.x;
-            else if (hb) stack[sp++] = ch.y;
+            if (ha || hb) {
+                if (ha && hb) {
+                    if (sp + 1 > LGPU_STACK) {
+                        atomicOr(S.err, 1);
+                        return hit;
+                    }
+                    const bool aFirst = an <= bn;
+                    stack[sp++] = aFirst ? ch.y : ch.x;
+                    e = aFirst ? ch.x : ch.y;
+                } else {
+                    e = ha ? ch.x : ch.y;
+                }
+                continue;
+            }
+#else
+            const float4 *np = reinterpret_cast<const float4 *>(S.nodes + ref);
+            const float4 h0 = ldg4(np);
+            const int4 h1 = ldg4i(reinterpret_cast<const int4 *>(np) + 1);
+            const int4 qa = ldg4i(reinterpret_cast<const int4 *>(np) + 2);
+            const int4 qb = ldg4i(reinterpret_cast<const int4 *>(np) + 3);
+            const int4 qc = ldg4i(reinterpret_cast<const int4 *>(np) + 4);
+            if (COUNT) st->nodes++;
+            uint32_t key[8];
+            wide_keys(h0, qa, qb, qc, o, inv, best, key);
+            if (key[0] != 0xffffffffu) {
+                int nhit = 1;
+#pragma unroll
+                for (int k = 1; k < 8; ++k) nhit += key[k] != 0xffffffffu ? 1 : 0;
+                if (sp + nhit - 1 > LGPU_STACK) {
+                    atomicOr(S.err, 1);
+                    return hit;
+                }
+#define LG_ENT(kk) ([&] {                                                                        \
+        const int ch = (int)((kk) & 7u);                                                          \
+        const uint32_t mb = ((uint32_t)(ch < 4 ? h1.z : h1.w) >> (8 * (ch & 3))) & 0xffu;         \
+        const int c = (int)(mb & 7u), off = (int)(mb >> 3);                                       \
+        return c ? (((h1.y + off) << LG_LEAF_BITS) | c) : ((h1.x + off) << LG_LEAF_BITS);         \
+    }())
+#pragma unroll
+                for (int k = 7; k >= 1; --k)
+                    if (key[k] != 0xffffffffu) stack[sp++] = LG_ENT(key[k]);
+                e = LG_ENT(key[0]);
+#undef LG_ENT
+                continue;
+            }
+#endif
         } else if (!in_blas) {
             /* TLAS leaf: one instance record */
             const DInst *I = S.insts + ref;
@@ -841,8 +928,13 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
             inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
             inst_obj = __ldg(&I->object);
             in_blas = true;
+            if (sp + 1 > LGPU_STACK) {
+                atomicOr(S.err, 1);
+                return hit;
+            }
             stack[sp++] = LG_MARKER;
-            stack[sp++] = __ldg(&I->root);
+            e = __ldg(&I->root);
+            continue;
         } else {
             for (int k = 0; k < cnt; ++k) {
                 const DTri *tp = S.tris + ref + k;
@@ -859,10 +951,8 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
                 }
             }
         }
-        if (sp >= LGPU_STACK - 2) {   /* depth is checked at commit; report instead of dropping nodes */
-            atomicOr(S.err, 1);
-            return hit;
-        }
+        if (sp == 0) break;
+        e = stack[--sp];
     }
     return hit;
 }

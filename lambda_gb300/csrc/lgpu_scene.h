@@ -4,7 +4,9 @@
  * Everything a kernel reads lives in a handful of flat arrays in HBM, addressed by 32-bit
  * indices, so one launch can hold ~100 M instanced triangles without per-object pointers:
  *
- *   BVH nodes   DNode  64 B  two child boxes in the parent (x/y/z rows) + two child refs
+ *   BVH nodes   DNode  64 B  binary node: both child boxes + child refs (default), or
+ *               DWide  80 B  8-wide node: eight child boxes quantised to 8 bits per plane against
+ *                            the node box, child records consecutive (built with LGPU_BVH_WIDE=1)
  *   triangles   DTri   48 B  v0, e1 = v1 - v0, e2 = v2 - v0 (Moller-Trumbore form), prim and
  *                            object ids in the w lanes; leaf triangles are contiguous
  *   instances   DInst  64 B  world->object 3x4 affine + BLAS root (TLAS leaves)
@@ -20,15 +22,47 @@
 
 #define LGPU_MAX_REGS 16
 #define LGPU_MAX_LEAVES 4
-#define LGPU_STACK 64
+/* traversal stack entries; the host computes each scene's exact worst case and refuses scenes
+ * above it */
+#define LGPU_STACK 96
+/* Node layout of the device BVH: 0 = binary nodes (DNode), 1 = 8-wide compressed nodes (DWide).
+ * The wide layout visits 2.7x fewer nodes on the 1080p terrain, but its traversal issues ~6x more
+ * instructions per visit with 8 of 32 lanes active, and measured slower there (193 vs 168 ms of
+ * traversal per frame; about even on the instanced volume scene), so binary nodes are the default. */
+#ifndef LGPU_BVH_WIDE
+#define LGPU_BVH_WIDE 0
+#endif
 
-/* BVH2 node: child c's box is (xs[2c], xs[2c+1]) etc.  ch = (ref0, count0, ref1, count1): count 0
- * means ref is an inner node index, count > 0 means ref is the first triangle record of a leaf
- * (BLAS) or the first instance record (TLAS). */
+/* BVH2 node (binned SAH build): child c's box is (xs[2c], xs[2c+1]) etc.
+ * ch = (ref0, ref1, -, -): ref = (index << 4) | count, count 0 for an inner node, else the first
+ * primitive record of a leaf of `count` primitives. */
 struct DNode {
     float4 xs, ys, zs;
     int4 ch;
 };
+
+/* 8-wide BVH node, 80 bytes (five 16-byte loads).  The node box's minimum corner p and per-axis
+ * power-of-two scales s = 2^(e - 127) define the child boxes: child k spans
+ * [p + qlo[a][k] * s_a, p + qhi[a][k] * s_a] on axis a.  The product q * s is exact, so host and
+ * device decode the same floats, and the builder rounds every plane outwards (the decoded box
+ * contains the child's true box).  Inner children are consecutive node records from child_base;
+ * leaf children's primitives are consecutive records from leaf_base.  meta[k]: bits 0-2 = the
+ * leaf's primitive count (0 for an inner child), bits 3-7 = offset from child_base (inner) or
+ * leaf_base (leaf).  Children k >= nchild are absent. */
+struct __align__(16) DWide {
+    float px, py, pz;
+    uint8_t ex, ey, ez, nchild;
+    int child_base, leaf_base;
+    uint8_t meta[8];
+    uint8_t qlo[3][8];
+    uint8_t qhi[3][8];
+};
+static_assert(sizeof(DWide) == 80, "DWide must be 80 bytes");
+#if LGPU_BVH_WIDE
+typedef DWide BvhNode;
+#else
+typedef DNode BvhNode;
+#endif
 
 struct DTri {
     float4 v0;   /* w = prim id (bits) */
@@ -146,7 +180,7 @@ struct DEnv {
 };
 
 struct DeviceScene {
-    const DNode *nodes;
+    const BvhNode *nodes;
     const DTri *tris;
     const DInst *insts;
     const DObject *objects;
