@@ -19,8 +19,13 @@ in oracle/_ref/ (git-ignored).
        IEEE single-precision results;
      * stb_image is compiled without its SIMD paths (STBI_NO_SIMD) for the same reason.
    Every edit is listed in EDITS with its reason.  Ids M* are mechanical (build only), S1 adds an
-   accessor the counter-based sampler needs, and B* patch the reference defects on the hot path;
-   the CPU oracle and the GPU module apply the same patches, so the three compute the same thing.
+   accessor the counter-based sampler needs, S2 the read-only accessors of the GPU module's
+   Lambda-side binding, and B* patch the reference defects on the hot path; the CPU oracle and the
+   GPU module apply the same patches, so the three compute the same thing.
+
+3. oracle/_ref/libref_binding.so -- the same units plus the GPU module's Lambda-side binding
+   (lambda_gb300/binding), which only compiles against Lambda's headers, linked with the module:
+   the tests drive the binding on lambda::Scene objects built by ref_li.cpp.
 
 The copy is made on a host that has the reference tree; where the tree is absent (a GPU host) a copy
 made earlier is compiled if present.
@@ -126,6 +131,34 @@ EDITS = [
      "\t\tReal Shift(const Real _point, const unsigned _dimensionIndex) const;",
      "\t\tReal Shift(const Real _point, const unsigned _dimensionIndex) const;\n\n"
      "\t\tinline unsigned GetPixelIndex() const { return pixelIndex; }"),
+    # S2: read-only accessors the GPU module's Lambda-side binding (lambda_gb300/binding) needs, the
+    # getters a maintainer adds with it: the camera frame, an instance's proxy and mesh, and the
+    # environment light's texture are not public
+    ("shading/graph/ShaderGraph.h", "B36", "output sockets lose their owning node: Node() links them, then every node "
+     "constructor overwrites them with MAKE_SOCKET, whose initialiser sets node = nullptr (GraphIterator, "
+     "ShaderGraph.cpp:130, then follows null); the binding reads the owner of a linked socket",
+     "MAKE_SOCKET_CALLBACK(_callback), nullptr, (_type)", "MAKE_SOCKET_CALLBACK(_callback), this, (_type)"),
+    ("shading/graph/GraphBxDF.h", "B36", "the same for the BxDF nodes' MAKE_BXDF_SOCKET",
+     "NodeDelegate::FromFunction<_DECLTYPE, _callback>(this), nullptr, (_type)",
+     "NodeDelegate::FromFunction<_DECLTYPE, _callback>(this), this, (_type)"),
+    ("camera/Camera.h", "S2", "binding: the camera frame and tan(fov / 2)",
+     "\t\tvoid SetFov(const Real _fov);",
+     "\t\tvoid SetFov(const Real _fov);\n\n"
+     "\t\tinline void GetFrame(Vec3 *_x, Vec3 *_y, Vec3 *_z, Real *_tanFov) const { *_x = xHat; *_y = yHat; *_z = zHat; *_tanFov = tanFov; }"),
+    ("core/Instance.h", "S2", "binding: the object an instance proxy wraps",
+     "\t\tvoid Commit(const RTCDevice &_device);\n",
+     "\t\tvoid Commit(const RTCDevice &_device);\n\n\t\tinline Object *GetObject() const { return iObject; }\n"),
+    ("core/Instance.h", "S2", "binding: the proxy an instance places",
+     "\t\tvoid Commit(const RTCDevice &_device) override;",
+     "\t\tvoid Commit(const RTCDevice &_device) override;\n\n\t\tinline InstanceProxy *GetProxy() const { return proxy; }"),
+    ("shading/TextureAdapter.h", "S2", "binding: the RGB texture behind an adapter (null for other kinds)",
+     "\t\tinline void operator=(TextureR32 *_rhs) { SetTexture(_rhs); }",
+     "\t\tinline void operator=(TextureR32 *_rhs) { SetTexture(_rhs); }\n\n"
+     "\t\tinline const Texture *GetRGBTexture() const { return textureType == TextureType::RGB ? reinterpret_cast<const Texture *>(texture) : nullptr; }"),
+    ("lighting/EnvironmentLight.h", "S2", "binding: the radiance map of an environment light",
+     "\t\tEnvironmentLight(Texture *_texture, const Real _intesity = 1);",
+     "\t\tEnvironmentLight(Texture *_texture, const Real _intesity = 1);\n\n"
+     "\t\tinline const TextureAdapter &GetRadianceMap() const { return radianceMap; }"),
     ("shading/media/HomogeneousMedium.cpp", "B2", "SampleEquiangular reads the uninitialised `t`",
      "const Real t = std::min(t, _event.hit->tFar);", "const Real t = std::min(dist, _event.hit->tFar);"),
     ("shading/media/HomogeneousMedium.cpp", "B3", "integer division makes PDFDistance zero",
@@ -345,6 +378,44 @@ def build_li(ref_root=None, force=False):
                    check=True)
     os.replace(tmp, LIB_LI)
     return LIB_LI
+
+
+LIB_BINDING = OUT / "libref_binding.so"
+BINDING = HERE.parent / "lambda_gb300" / "binding"
+GPU_LIB_DIR = HERE.parent / "lambda_gb300" / "_build"
+
+
+def build_binding(ref_root=None, force=False):
+    """The GPU module's Lambda-side binding (lambda_gb300/binding/lambda_gpu_binding.cpp) compiled
+    against the patched copy and linked with the integrator library's units, ref_li.cpp built with
+    REF_WITH_BINDING, and the module (lambda_gb300/_build/liblambda_gpu.so, found through the
+    library's run path).  Returns its path, or None when no copy or no module library exists."""
+    if build_li(ref_root) is None or not (GPU_LIB_DIR / "liblambda_gpu.so").exists():
+        return None
+    obj_dir = OUT / "li_obj"
+    srcs = [(HERE / "ref_li.cpp", obj_dir / "ref_li_binding.o", ["-DREF_WITH_BINDING"]),
+            (BINDING / "lambda_gpu_binding.cpp", obj_dir / "lambda_gpu_binding.o", [])]
+    deps = [BINDING / "lambda_gpu_binding.h", BINDING / "lambda_gpu_binding.cpp", HERE / "ref_li.cpp", LIB_LI,
+            GPU_LIB_DIR / "liblambda_gpu.so"]
+    if LIB_BINDING.exists() and not force and all(LIB_BINDING.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return LIB_BINDING
+
+    def one(job):
+        src, obj, extra = job
+        r = subprocess.run(_li_flags() + extra + ["-c", str(src), "-o", str(obj)], capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError("binding build failed on %s:\n%s" % (src, r.stderr[-4000:]))
+
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        list(ex.map(one, srcs))
+    objs = [obj_dir / (u.replace("/", "_") + ".o") for u in LI_UNITS] + [obj_dir / "rtcore_bvh.o"]
+    objs += [o for _, o, _ in srcs]
+    tmp = LIB_BINDING.with_suffix(".so.tmp%d" % os.getpid())
+    rpath = os.path.relpath(GPU_LIB_DIR, OUT)
+    subprocess.run(["g++", "-shared", "-o", str(tmp), *[str(o) for o in objs], "-L" + str(GPU_LIB_DIR), "-llambda_gpu",
+                    "-Wl,-rpath,$ORIGIN/" + rpath, "-lpthread", "-Wl,--no-undefined"], check=True)
+    os.replace(tmp, LIB_BINDING)
+    return LIB_BINDING
 
 
 if __name__ == "__main__":

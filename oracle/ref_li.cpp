@@ -17,10 +17,15 @@
  *                   through the reference's RenderMosaic + TileRenderers::UniformSpp on a pool of
  *                   std::threads (the TBB/OpenMP mosaic renderers are not built)
  *   ref_render_tiles   the same tile renderer over a caller-chosen subset of tiles (timing samples)
+ *   ref_binding_*   (built with REF_WITH_BINDING into libref_binding.so) the GPU module's Lambda-side
+ *                   binding on the scene built here: translation check and renders through it
  *   ref_kat_*       function-level known answers of reference units that need a scene or graph
  */
 #include "../include/lambda_gpu.h"
 #include "../lambda_gb300/csrc/lgpu_rng.h"
+#ifdef REF_WITH_BINDING
+#include "../lambda_gb300/binding/lambda_gpu_binding.h"
+#endif
 
 #include <camera/Camera.h>
 #include <camera/Film.h>
@@ -51,6 +56,7 @@
 #include <shading/media/HomogeneousMedium.h>
 
 #include <atomic>
+#include <cstring>
 #include <iostream>
 #include <memory>
 #include <streambuf>
@@ -569,5 +575,75 @@ __attribute__((visibility("default"))) int ref_render_tiles(void *h, const lgpu_
                                                             const int32_t *tiles, int n_tiles, float *film, int threads) {
     return render_tiles(*static_cast<RefScene *>(h), cd, o, tiles, n_tiles, film, threads);
 }
+
+#ifdef REF_WITH_BINDING
+/* The GPU module's Lambda-side binding (lambda_gb300/binding) run on the lambda::Scene built here:
+ * the translation back to a scene description, checked on the host (lgpu_scene_check), and
+ * renders through its RenderDirective and TileRenderer entry points. */
+
+/* counts: meshes, objects, materials, nodes, lights, media, textures, has_volumes, light_strategy */
+__attribute__((visibility("default"))) int ref_binding_check(void *h, char *report, size_t report_size, int32_t *counts) {
+    RefScene &R = *static_cast<RefScene *>(h);
+    lambda_gpu::SceneDesc sd;
+    const int rc = sd.Build(R.scene);
+    if (rc != LGPU_OK) {
+        g_err = sd.Error();
+        if (report && report_size) { std::strncpy(report, g_err.c_str(), report_size - 1); report[report_size - 1] = 0; }
+        return rc;
+    }
+    const lgpu_scene_desc &d = sd.Desc();
+    const int32_t c[9] = {d.num_meshes, d.num_objects, d.num_materials, d.num_nodes, d.num_lights, d.num_media,
+                          d.num_textures, d.has_volumes, d.light_strategy};
+    for (int k = 0; k < 9; ++k) counts[k] = c[k];
+    return lgpu_scene_check(&d, report, report_size);
+}
+
+/* mode 0: GpuRenderer::RenderDirective over the whole film; mode 1: RenderMosaic's 16 x 16 tiles
+ * through GpuTileRenderer.  film_out: height x width x 4 (summed rgb, samples). */
+__attribute__((visibility("default"))) int ref_binding_render(void *h, const lgpu_camera_desc *cd, const lgpu_render_opts *o,
+                                                              int mode, float *film_out) {
+    RefScene &R = *static_cast<RefScene *>(h);
+    RefCamera rc;
+    if (!make_camera(*cd, o->width, o->height, rc)) return LGPU_ERR_INVALID_ARG;
+    CounterSampler proto;
+    proto.seed = o->seed;
+    std::shared_ptr<Integrator> integ = make_integrator(*o, &proto);
+    if (!integ) { g_err = "integrator not driven here"; return LGPU_ERR_INVALID_ARG; }
+    Film film(o->width, o->height);
+    SampleShifter shifter(nullptr);
+    RenderDirective dir;
+    dir.film = &film;
+    dir.scene = &R.scene;
+    dir.camera = rc.cam.get();
+    dir.integrator = integ.get();
+    dir.sampler = &proto;
+    dir.sampleShifter = &shifter;
+    dir.tileSizeX = dir.tileSizeY = 16;
+    dir.spp = o->spp;
+    lambda_gpu::GpuRenderer gpu(0);
+    gpu.seed = o->seed;
+    gpu.kernelMode = o->kernel_mode;
+    int r = gpu.Commit(R.scene);
+    if (r == LGPU_OK) {
+        if (mode == 0) {
+            r = gpu.RenderDirective(dir);
+        } else {
+            RenderMosaic mosaic(dir);
+            lambda_gpu::SetTileRenderer(&gpu);
+            for (RenderTile &t : mosaic.tiles) lambda_gpu::GpuTileRenderer(&t);
+            r = lambda_gpu::TileRendererError();
+            lambda_gpu::SetTileRenderer(nullptr);
+        }
+    }
+    if (r != LGPU_OK) { g_err = gpu.LastError(); return r; }
+    for (int y = 0; y < o->height; ++y)
+        for (int x = 0; x < o->width; ++x) {
+            const FilmPixel &p = film.filmData.GetPixelCoord(x, y);
+            float *f = film_out + 4 * ((size_t)y * o->width + x);
+            f[0] = p.spectrum[0]; f[1] = p.spectrum[1]; f[2] = p.spectrum[2]; f[3] = (float)p.nSamples;
+        }
+    return LGPU_OK;
+}
+#endif
 
 }  // extern "C"
