@@ -40,8 +40,8 @@ UNIT = "Mpath-samples/s"
 WORKLOAD = dict(workload="many-light terrain (2.1M tris, 10k emitters, sky env), MIS volumetric path tracing",
                 width=1920, height=1080, spp=64, max_depth=6, triangles=2093058 + 10000, emitters=10000,
                 spectral="RGB3", light_sampler="light tree")
-# DRAM bytes (read + write) per unit of work (resumed path, traced ray) of the wavefront kernels,
-# from one ncu capture of a 480x270x16 frame of the same scene (profiles/wavefront_terrain_1080p.md);
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of work (resumed path, traced
+# ray) of the wavefront kernels, from one ncu capture of a 480x270x16 frame of the same scene,
 # multiplied by the units of an average launch of the timed run.
 NCU_DRAM_BYTES_PER_UNIT = {"k_wave_resume": 876.0, "k_wave_trace": 645.0}
 # Algorithmic bytes per unit: a resumed path reads and writes its path state (96 B each way: ray,

@@ -61,7 +61,7 @@ struct lgpu_context {
     void *w_cold = nullptr;
     size_t w_state_bytes = 0;
     size_t w_slots = 0;
-    float4 *w_qo = nullptr, *w_qd = nullptr, *w_res = nullptr;
+    float4 *w_qo = nullptr, *w_qd = nullptr, *w_res = nullptr, *w_trout = nullptr;
     int *w_resobj = nullptr, *w_qa = nullptr, *w_qb = nullptr, *w_counts = nullptr, *w_free = nullptr;
     unsigned long long *w_next = nullptr;
     int *h_count = nullptr;   /* pinned */
@@ -376,6 +376,7 @@ LGPU_API void lgpu_destroy(lgpu_context *c) {
     cudaFree(c->d_views);
     if (c->graph_stream) cudaStreamDestroy(c->graph_stream);
     cudaFree(c->w_states); cudaFree(c->w_cold); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
+    cudaFree(c->w_trout);
     cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_counts); cudaFree(c->w_next); cudaFree(c->w_paths); cudaFree(c->w_free);
     if (c->h_count) cudaFreeHost(c->h_count);
     delete c;
@@ -998,14 +999,33 @@ int check_opts(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_render_o
     return check_camera(c, cam);
 }
 
+/* Transmittance walks run inside the trace kernel (WaveArgs::fold_tr) for RGB3 renders, whose
+ * spectra the trace kernel computes in; a build with -DLGPU_NO_FOLD_TR keeps one resume per
+ * segment for comparison. */
+int fold_tr(const lgpu_render_opts *o) {
+#ifdef LGPU_NO_FOLD_TR
+    (void)o;
+    return 0;
+#else
+    return o->spectral_mode == LGPU_SPECTRAL_RGB3 ? 1 : 0;
+#endif
+}
+
+/* Kernel launches of one trace step over m queries (the walk segment runs in its own kernel). */
+int trace_launches(const WaveArgs &W, int m) {
+    const int split = W.fold_tr ? W.seg_off[LG_NSEG - 1] : m;
+    return (split > 0 ? 1 : 0) + (m > split ? 1 : 0);
+}
+
 /* Grow the wavefront pool to `slots` path slots of `state_bytes` each. */
 int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes, size_t cold_bytes) {
     if (c->w_slots >= slots && c->w_state_bytes == state_bytes) return LGPU_OK;
     cudaFree(c->w_cold);
     c->w_cold = nullptr;
     cudaFree(c->w_states); cudaFree(c->w_qo); cudaFree(c->w_qd); cudaFree(c->w_res); cudaFree(c->w_resobj);
-    cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_free);
-    c->w_states = nullptr; c->w_qo = c->w_qd = c->w_res = nullptr; c->w_resobj = c->w_qa = c->w_qb = c->w_free = nullptr;
+    cudaFree(c->w_qa); cudaFree(c->w_qb); cudaFree(c->w_free); cudaFree(c->w_trout);
+    c->w_states = nullptr; c->w_qo = c->w_qd = c->w_res = c->w_trout = nullptr;
+    c->w_resobj = c->w_qa = c->w_qb = c->w_free = nullptr;
     c->w_slots = 0;
     cudaError_t e = cudaMalloc(&c->w_states, slots * state_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->w_cold, slots * cold_bytes);
@@ -1013,6 +1033,7 @@ int ensure_pool(lgpu_context *c, size_t slots, size_t state_bytes, size_t cold_b
     if (e == cudaSuccess) e = cudaMalloc(&c->w_qd, slots * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_res, slots * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_resobj, slots * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->w_trout, 2 * slots * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_qa, LG_NSEG * slots * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_qb, LG_NSEG * slots * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&c->w_free, slots * sizeof(int));
@@ -1076,7 +1097,7 @@ int run_graph_loop(lgpu_context *c, WaveArgs &W, bool hero, size_t slots, uint64
     int rc = LGPU_OK;
     for (;;) {
         for (int k = 0; k < 2 && e == cudaSuccess; ++k) { e = cudaGraphLaunch(ge, st); ++replays; }
-        launches += 2 * 2 * (1 + LG_NSEG + 2);
+        launches += 2 * 2 * ((W0.fold_tr ? 2 : 1) + LG_NSEG + 2);
         if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_count, ca, LG_NSEG * sizeof(int), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) { rc = cuda_fail(c, e, "graph replay"); break; }
@@ -1127,6 +1148,8 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     W.states = c->w_states;
     W.cold = c->w_cold;
     W.qo = c->w_qo; W.qd = c->w_qd; W.res = c->w_res; W.res_obj = c->w_resobj;
+    W.tr_out = c->w_trout;
+    W.fold_tr = fold_tr(o);
     W.next_path = c->w_next;
     W.n_paths = n;
     W.base = base;
@@ -1207,7 +1230,7 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
         e = count ? wave_trace_3_1(W, m, st, tblock) : wave_trace_3_0(W, m, st, tblock);
         cudaEventRecord(ev[1], st);
         c->stats.traced += (uint64_t)m;
-        launches += 1;
+        launches += trace_launches(W, m);
         /* one resume launch per queue segment: each launch enters the state machine at one
          * program point, so its warps run the same code */
         const WaveArgs W0 = W;
@@ -1761,6 +1784,7 @@ LGPU_API int lgpu_adjoint(lgpu_context *c, const lgpu_camera_desc *cam, const lg
  *   cold path state  S x max(sizeof PCold<3>, PCold<4>)
  *   ray origin, ray direction, hit record   3 x S x 16 B
  *   hit object, free list                   2 x S x 4 B
+ *   transmittance-walk results              2 x S x 16 B
  *   stage queues A and B                    2 x LG_NSEG x S x 4 B
  *   queue counts, free count                (2 x LG_NSEG + 2) x 4 B
  *   next-path counter                       8 B
@@ -1778,7 +1802,8 @@ constexpr size_t NA_OFF_QO = NA_OFF_COLD + na_round(NA_COLD * NA_SLOTS);
 constexpr size_t NA_OFF_QD = NA_OFF_QO + na_round(16 * NA_SLOTS);
 constexpr size_t NA_OFF_RES = NA_OFF_QD + na_round(16 * NA_SLOTS);
 constexpr size_t NA_OFF_RESOBJ = NA_OFF_RES + na_round(16 * NA_SLOTS);
-constexpr size_t NA_OFF_FREE = NA_OFF_RESOBJ + na_round(4 * NA_SLOTS);
+constexpr size_t NA_OFF_TROUT = NA_OFF_RESOBJ + na_round(4 * NA_SLOTS);
+constexpr size_t NA_OFF_FREE = NA_OFF_TROUT + na_round(2 * 16 * NA_SLOTS);
 constexpr size_t NA_OFF_QA = NA_OFF_FREE + na_round(4 * NA_SLOTS);
 constexpr size_t NA_OFF_QB = NA_OFF_QA + na_round(4 * LG_NSEG * NA_SLOTS);
 constexpr size_t NA_OFF_COUNTS = NA_OFF_QB + na_round(4 * LG_NSEG * NA_SLOTS);
@@ -1842,6 +1867,8 @@ LGPU_API int lgpu_render_paths_noalloc(lgpu_context *c, const lgpu_camera_desc *
     W.qd = reinterpret_cast<float4 *>(base + NA_OFF_QD);
     W.res = reinterpret_cast<float4 *>(base + NA_OFF_RES);
     W.res_obj = reinterpret_cast<int *>(base + NA_OFF_RESOBJ);
+    W.tr_out = reinterpret_cast<float4 *>(base + NA_OFF_TROUT);
+    W.fold_tr = fold_tr(o);
     W.free_list = reinterpret_cast<int *>(base + NA_OFF_FREE);
     W.next_path = reinterpret_cast<unsigned long long *>(base + NA_OFF_NEXT);
     W.n_paths = n;
@@ -1908,6 +1935,7 @@ LGPU_API int lgpu_render_paths_noalloc(lgpu_context *c, const lgpu_camera_desc *
         e = cudaMemsetAsync(cb, 0, LG_NSEG * sizeof(int), st);
         W.queue_in = qa; W.queue_out = qb; W.count_out = cb;
         if (e == cudaSuccess) e = wave_trace_3_0(W, m, st);
+        launches += trace_launches(W, m);
         const WaveArgs W0 = W;
         for (int k = 0; k < LG_NSEG && e == cudaSuccess; ++k) {   /* one resume launch per stage */
             const int nk = W0.seg_off[k + 1] - W0.seg_off[k];
@@ -1923,7 +1951,7 @@ LGPU_API int lgpu_render_paths_noalloc(lgpu_context *c, const lgpu_camera_desc *
         if (e == cudaSuccess) e = resume(m, 1);   /* new paths into the freed slots */
         if (e != cudaSuccess) return failed(0, e, "wavefront iteration");
         c->stats.traced += (uint64_t)m;
-        launches += 3;
+        launches += 2;
         std::swap(qa, qb);
         std::swap(ca, cb);
     }

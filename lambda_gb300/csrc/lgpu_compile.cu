@@ -71,10 +71,6 @@ void build_bvh(const std::vector<Aabb> &boxes, int max_leaf, int node_base, int 
     }
     uint32_t *idx = out.order.data();
     const int NB = 16;
-    /* inner node records: box of each child filled in when the child is processed */
-    struct Tmp { Aabb box; int ref; };
-    std::vector<Tmp> tmpChild;   /* unused */
-    (void)tmpChild;
     out.nodes.reserve(2 * (size_t)n / std::max(1, max_leaf) + 16);
     /* a job describes a range that must become child `slot` of parent `node` */
     struct Job { int parent, slot, first, count, depth; };

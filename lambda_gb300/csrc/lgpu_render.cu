@@ -481,23 +481,73 @@ size_t LG_CAT(wave_cold_bytes_, LGPU_NS, LGPU_COUNT)() { return sizeof(PCold<LGP
 
 #if LGPU_NS == 3 && LG_PART(3)
 /* Answer every queued query: closest hit (Scene::Intersect) or occlusion (rtcOccluded1). */
-template <bool COUNT, int BS, bool DEV>
-__global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveArgs W, int n) {
+/* Scene::IntersectTr (Scene.cpp:45-81) as one query: closest hits through surfaces without a BxDF
+ * or light, each segment's homogeneous transmittance multiplied in and the medium switched at the
+ * boundary, until a surface stops it, maxT is passed (o.w >= 0), the ray escapes, or 256 segments.
+ * Every step computes what the resume's PC_TR_STEP computes, in the same order (RGB3 spectra). */
+template <bool COUNT, class STK>
+__device__ __forceinline__ void tr_walk(const WaveArgs &W, int slot, float4 qo, float4 qd, TravStats *st, STK &stk) {
+    const DeviceScene &S = W.S;
+    float3 o = make_float3(qo.x, qo.y, qo.z);
+    const float3 d = make_float3(qd.x, qd.y, qd.z);
+    const float maxT = qo.w;
+    int med = (__float_as_int(qd.w) >> 8) - 1;
+    Spec<3> Tr(1.f);
+    float tFar = 0.f;
+    int flags = 0;
+    HitRec last;
+    last.t = finf(); last.u = last.v = 0.f; last.prim = 0; last.obj = -1;
+    float3 lastO = o;
+    for (int iter = 0;;) {
+        HitRec hr;
+        const bool ok = traverse_t<COUNT>(S, o, d, finf(), false, &hr, st, stk);
+        if (!ok || !(hr.obj >= 0 && hr.t > 0.f && hr.t < finf())) break;
+        RayHit h;
+        process_hit(S, o, d, hr, h);
+        flags |= 2;
+        last = hr;
+        lastO = o;
+        tFar += h.tFar;
+        bool term = false;
+        if (maxT >= 0.f) {
+            term = tFar > maxT;
+            if (term) { const float delta = tFar - maxT; tFar -= delta; h.tFar -= delta; }
+        }
+        if (med >= 0) Tr *= medium_tr<3>(S.media[med], h.tFar);
+        const DMaterial &m = S.materials[S.objects[h.obj].material];
+        if (term || m.has_bsdf || m.light >= 0) { flags |= 1; break; }
+        med = dot(d, h.nG) < 0.f ? m.medium_interior : m.medium_exterior;
+        o = h.point + h.nG * (dot(h.nG, d) < 0.f ? -SURFACE_EPSILON : SURFACE_EPSILON);
+        if (++iter >= 256) break;
+    }
+    const float4 a = Tr.as4();
+    W.tr_out[2 * slot] = make_float4(a.x, a.y, a.z, tFar);
+    W.tr_out[2 * slot + 1] = make_float4(lastO.x, lastO.y, lastO.z, __int_as_float(flags));
+    W.res[slot] = make_float4(last.t, last.u, last.v, __int_as_float(last.prim));
+    W.res_obj[slot] = last.obj;
+}
+
+/* Queries [lo, n) of the input queue (segments back to back).  WALK = false: closest hits and
+ * occlusion; WALK = true: the transmittance walks of the last segment, whose longer code would
+ * otherwise raise every query's register count (86 against 64). */
+template <bool COUNT, int BS, bool DEV, bool WALK>
+__global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveArgs W, int lo, int n) {
     LocalStack stk;   /* measured faster than a shared-memory column stack (L1 serves it) */
     int off[LG_NSEG + 1];
     if (DEV) {   /* device-driven: segment sizes from the device */
         off[0] = 0;
 #pragma unroll
         for (int k = 0; k < LG_NSEG; ++k) off[k + 1] = off[k] + W.count_in[k];
-        n = off[LG_NSEG];
+        lo = WALK ? off[LG_NSEG - 1] : 0;
+        n = (WALK || !W.fold_tr) ? off[LG_NSEG] : off[LG_NSEG - 1];
     } else {
 #pragma unroll
         for (int k = 0; k <= LG_NSEG; ++k) off[k] = W.seg_off[k];
     }
     const int stride = DEV ? W.cap : W.cap_in;
     TravStats st = {0u, 0u, 0u};
-    const int step = DEV ? gridDim.x * blockDim.x : n;   /* host-sized launches run the body once */
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
+    const int step = DEV ? gridDim.x * blockDim.x : n - lo;   /* host-sized launches run the body once */
+    for (int i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
         int seg = 0, first = 0;
 #pragma unroll
         for (int k = 1; k < LG_NSEG; ++k) seg += (i >= off[k]) ? 1 : 0;
@@ -506,7 +556,10 @@ __global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveA
         const int slot = W.queue_in[seg * stride + (i - first)];
         const float4 o = W.qo[slot], d = W.qd[slot];
         HitRec hr;
-        if (__float_as_int(d.w) == Q_CLOSEST) {
+        const int qtype = __float_as_int(d.w) & 0xff;
+        if (WALK) {
+            tr_walk<COUNT>(W, slot, o, d, &st, stk);
+        } else if (qtype == Q_CLOSEST) {
             const bool ok = traverse_t<COUNT>(W.S, make_float3(o.x, o.y, o.z), make_float3(d.x, d.y, d.z), finf(), false, &hr, &st, stk);
             W.res[slot] = ok ? make_float4(hr.t, hr.u, hr.v, __int_as_float(hr.prim)) : make_float4(finf(), 0.f, 0.f, 0.f);
             W.res_obj[slot] = ok ? hr.obj : -1;
@@ -526,20 +579,30 @@ __global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveA
         }
     }
 }
-/* n < 0: device-driven launch over a resident grid (the queue sizes are read on the device);
- * n == 0: set-up of the resident grid only.  block: 64, 128, 256 or 512 threads. */
+/* n < 0: device-driven launches over resident grids (the queue sizes are read on the device);
+ * n == 0: set-up of the resident grids only.  With folded transmittance walks (W.fold_tr) the
+ * last segment goes to the WALK kernel, the others to the plain one.  block: 64, 128, 256 or 512. */
 template <int BS>
 static cudaError_t trace_launch(const WaveArgs &W, int n, cudaStream_t st) {
-    static std::atomic<int> grids[LG_MAX_DEVICES];
+    static std::atomic<int> grids[LG_MAX_DEVICES], walk_grids[LG_MAX_DEVICES];
     const int dev = current_device();
     int grid = grids[dev].load(std::memory_order_acquire);
-    if (!grid) {   /* n == 0: set-up only */
-        grid = resident_grid(k_wave_trace<LGPU_COUNT != 0, BS, true>, BS, 0);
+    int wgrid = walk_grids[dev].load(std::memory_order_acquire);
+    if (!grid || !wgrid) {   /* n == 0: set-up only */
+        grid = resident_grid(k_wave_trace<LGPU_COUNT != 0, BS, true, false>, BS, 0);
+        wgrid = resident_grid(k_wave_trace<LGPU_COUNT != 0, BS, true, true>, BS, 0);
         grids[dev].store(grid, std::memory_order_release);
+        walk_grids[dev].store(wgrid, std::memory_order_release);
     }
     if (n == 0) return cudaSuccess;
-    if (n < 0) k_wave_trace<LGPU_COUNT != 0, BS, true><<<grid, BS, 0, st>>>(W, 0);
-    else k_wave_trace<LGPU_COUNT != 0, BS, false><<<(n + BS - 1) / BS, BS, 0, st>>>(W, n);
+    if (n < 0) {
+        k_wave_trace<LGPU_COUNT != 0, BS, true, false><<<grid, BS, 0, st>>>(W, 0, 0);
+        if (W.fold_tr) k_wave_trace<LGPU_COUNT != 0, BS, true, true><<<wgrid, BS, 0, st>>>(W, 0, 0);
+        return cudaGetLastError();
+    }
+    const int split = W.fold_tr ? W.seg_off[LG_NSEG - 1] : n;
+    if (split > 0) k_wave_trace<LGPU_COUNT != 0, BS, false, false><<<(split + BS - 1) / BS, BS, 0, st>>>(W, 0, split);
+    if (n > split) k_wave_trace<LGPU_COUNT != 0, BS, false, true><<<(n - split + BS - 1) / BS, BS, 0, st>>>(W, split, n);
     return cudaGetLastError();
 }
 cudaError_t LG_CAT(wave_trace_, LGPU_NS, LGPU_COUNT)(const WaveArgs &W, int n, cudaStream_t st, int block) {

@@ -23,7 +23,9 @@ namespace lg {
 
 namespace cgx = cooperative_groups;
 
-enum : int { Q_CLOSEST = 1, Q_OCCL = 2 };
+/* Query types (low byte of the direction record's w; a transmittance walk keeps its medium + 1 in
+ * the bits above). */
+enum : int { Q_CLOSEST = 1, Q_OCCL = 2, Q_TR = 3 };
 
 enum : int {
     PC_NEW = 0, PC_LOOP, PC_TOP_HIT, PC_MISS, PC_BODY, PC_SURF_A, PC_SURF_LI, PC_SURF_EXT, PC_NULL_EXT,
@@ -127,6 +129,12 @@ struct WaveArgs {
     const int *count_in;
     int seg_sel;                  /* device-driven resume: the one segment this launch continues */
     unsigned long long *counters; /* traversal counters (COUNT variant) */
+    /* Transmittance walks folded into the trace kernel (RGB3 renders): a Q_TR query runs the whole
+     * Scene::IntersectTr loop there and leaves, per slot, tr_out[2 slot] = (Tr, accumulated
+     * distance) and tr_out[2 slot + 1] = (origin of the last segment, flags: 1 = stopped on a
+     * surface, 2 = a segment was hit), with the last segment's hit in res / res_obj. */
+    float4 *tr_out;
+    int fold_tr;
 };
 
 /* Append `slot` to segment `seg` of the next queue; one atomic per group of lanes with the same
@@ -178,7 +186,8 @@ struct Wave {
         c.trO = o; c.trD = d; c.trMed = med; c.trTarget = target; c.trMaxT = maxT; c.trRet = ret;
         c.trTFar = 0.f; c.trIter = 0; s.trTr = Spec<NS>(1.f);
         if (target == TR_TEMP) s.tmpTFar = finf();
-        issue(o, d, finf(), Q_CLOSEST, PC_TR_STEP);
+        if (NS == 3 && W.fold_tr) issue(o, d, maxT, Q_TR | ((med + 1) << 8), PC_TR_STEP);   /* the whole walk */
+        else issue(o, d, finf(), Q_CLOSEST, PC_TR_STEP);
     }
     /* Light::MutualVisibility / PointMutualVisibility / RayEscapes (Light.cpp:10-49) */
     __device__ void start_vis(float3 o, float3 d, float m, int mode, int ret) {
@@ -642,6 +651,26 @@ struct Wave {
             case PC_TR_STEP: {   /* one segment of Scene::IntersectTr (Scene.cpp:45-81) */
                 auto t = T();
                 HitRec hr;
+                if (NS == 3 && W.fold_tr) {
+                    /* the trace kernel ran the whole walk: the state its last step leaves */
+                    const float4 a = W.tr_out[2 * slot], b = W.tr_out[2 * slot + 1];
+                    const int fl = __float_as_int(b.w);
+                    s.trTr = Spec<NS>::from4(a);
+                    c.trTFar = a.w;
+                    s.trResult = fl & 1;
+                    if (fl & 2) {
+                        closest(hr);
+                        const float fin = (fl & 1) ? c.trTFar : hr.t;   /* h.tFar the last step left */
+                        if (c.trTarget == TR_EVENT) {
+                            process_hit(S, mk(b.x, b.y, b.z), c.trD, hr, s.hit);
+                            s.hit.tFar = fin;
+                        } else {
+                            s.tmpTFar = fin;
+                        }
+                    }
+                    s.pc = c.trRet;
+                    break;
+                }
                 if (!closest(hr)) { s.trResult = 0; s.pc = c.trRet; break; }
                 RayHit tmp;
                 RayHit &h = c.trTarget == TR_EVENT ? s.hit : tmp;
