@@ -43,7 +43,7 @@ WORKLOAD = dict(workload="many-light terrain (2.1M tris, 10k emitters, sky env),
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of work (resumed path, traced
 # ray) of the wavefront kernels, from one ncu capture of a 480x270x16 frame of the same scene,
 # multiplied by the units of an average launch of the timed run.
-NCU_DRAM_BYTES_PER_UNIT = {"k_wave_resume": 876.0, "k_wave_trace": 645.0}
+NCU_DRAM_BYTES_PER_UNIT = {"k_wave_resume": 858.0, "k_wave_trace": 79.5}
 # Algorithmic bytes per unit: a resumed path reads and writes its path state (96 B each way: ray,
 # throughput, radiance, pdfs, medium, depth, ids); a traced ray fetches its BVH nodes and triangle
 # records (counted in-kernel) plus 32 B of ray and 20 B of hit record.

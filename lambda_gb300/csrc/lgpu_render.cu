@@ -530,8 +530,17 @@ __device__ __forceinline__ void tr_walk(const WaveArgs &W, int slot, float4 qo, 
 /* Queries [lo, n) of the input queue (segments back to back).  WALK = false: closest hits and
  * occlusion; WALK = true: the transmittance walks of the last segment, whose longer code would
  * otherwise raise every query's register count (86 against 64). */
+/* LGPU_TRACE_MINW: resident warps per SM the plain trace kernel is compiled for.  36 (56 registers
+ * at 64 threads, 12 B of spills) measured 13 % faster on the 1080p terrain than the compiler's own
+ * choice (64 registers, 28 warps) and 2 % faster than 40 (48 registers); 0 leaves it to the
+ * compiler.  The walk kernel keeps the compiler's choice (it would spill 284 B at 56). */
+#ifndef LGPU_TRACE_MINW
+#define LGPU_TRACE_MINW 36
+#endif
+#define LG_TRACE_MINB(BS, WALK) ((!(WALK) && LGPU_TRACE_MINW / ((BS) / 32) > 0) ? LGPU_TRACE_MINW / ((BS) / 32) : 1)
+
 template <bool COUNT, int BS, bool DEV, bool WALK>
-__global__ void __launch_bounds__(BS) k_wave_trace(const __grid_constant__ WaveArgs W, int lo, int n) {
+__global__ void __launch_bounds__(BS, LG_TRACE_MINB(BS, WALK)) k_wave_trace(const __grid_constant__ WaveArgs W, int lo, int n) {
     LocalStack stk;   /* measured faster than a shared-memory column stack (L1 serves it) */
     int off[LG_NSEG + 1];
     if (DEV) {   /* device-driven: segment sizes from the device */

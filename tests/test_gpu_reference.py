@@ -8,9 +8,11 @@ on twelve seeded scenes -- the three benchmark configurations at full size (1080
 light type, both light samplers and the path / volumetric-path integrators.
 
 Criterion: RGB within 1e-4 relative (1e-6 absolute floor) and the same number of random numbers
-drawn, on at least 99.9 % of paths.  The GPU contracts a*b+c into fused multiply-adds where the
-reference rounds twice; a path whose Russian-roulette or lobe decision sits within that rounding of
-its threshold can take the other branch, and the test lists every such path it finds.
+drawn, on at least 99.9 % of paths.  The device code rounds every product and sum as the reference
+does (no multiply-add contraction), but its transcendental functions (exp, log, sin, cos, pow, tan)
+are CUDA's, not the host C library's, and can differ in the last bit; a path whose Russian-roulette
+or lobe decision sits within that difference of its threshold takes the other branch, and the test
+lists every such path it finds.
 """
 import numpy as np
 import pytest
