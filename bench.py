@@ -723,6 +723,16 @@ def main():
             "kernels": kernels, "nodes_visited": stats["nodes_visited"], "tris_tested": stats["tris_tested"],
             "rays": stats["rays"], "mrays_per_s": stats["rays"] / mean_kernel_s / 1e6,
             "step_ms": float(np.mean(kernel_ms))}
+    # the traversal's node and triangle records are served from L2: its roofline is the L2 read
+    # peak, measured here (after the timed region) by the module's own read kernel on a 32 MiB
+    # buffer; a 4 GiB read beside it checks the probe against the HBM copy peak
+    l2 = r.probe_bandwidth(32 << 20, 400)
+    hbm_read = r.probe_bandwidth(4 << 30, 5)
+    tk = kernels.get("k_wave_trace")
+    roof["l2"] = {"peak_gbs": l2, "hbm_read_gbs": hbm_read, "probe": "lgpu_probe_bandwidth: ld.global.cg float4 reads, "
+                  "32 MiB x 400 passes (L2) and 4 GiB x 5 (HBM), one launch each",
+                  "trace_achieved_gbs": tk["achieved_gbs"] if tk else None,
+                  "trace_frac": tk["achieved_gbs"] / l2 if (tk and l2 > 0) else None}
     cpu = None
     if not args.no_cpu:
         cpu = cpu_baseline(sb, cam, opts, args.cpu_seconds, gpu=r)

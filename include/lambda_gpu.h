@@ -485,6 +485,14 @@ LGPU_API int lgpu_get_stats(const lgpu_context *ctx, lgpu_stats *out);
 /* Version string of the module. */
 LGPU_API const char *lgpu_version(void);
 
+/* Read bandwidth of this device for a buffer of `bytes` (rounded down to 16 B): the buffer is
+ * allocated, zeroed and read once to warm the caches, then read `reps` times in one launch of a
+ * read-only kernel of the module (loads cached in L2 only), timed with CUDA events;
+ * *gbs = bytes * reps / time.
+ * A buffer well inside L2 (e.g. 32 MiB) gives the L2 read peak that the traversal kernels are
+ * compared against; one well beyond it gives the HBM read rate.  No counterpart in the reference. */
+LGPU_API int lgpu_probe_bandwidth(lgpu_context *ctx, uint64_t bytes, int32_t reps, double *gbs);
+
 #ifdef __cplusplus
 }
 #endif

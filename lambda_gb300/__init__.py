@@ -19,7 +19,7 @@ LIB_PATH = pathlib.Path(os.environ["LGPU_LIB_PATH"]) if os.environ.get("LGPU_LIB
 EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_scene_commit", "lgpu_render",
            "lgpu_render_device", "lgpu_render_paths", "lgpu_render_count", "lgpu_intersect",
            "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc", "lgpu_render_batch", "lgpu_autotune", "lgpu_adjoint", "lgpu_film_resolve",
-           "lgpu_render_progressive"]
+           "lgpu_render_progressive", "lgpu_probe_bandwidth"]
 
 _lib = None
 
@@ -59,6 +59,7 @@ def lib():
         L.lgpu_intersect.argtypes = [vp, vp, vp, vp, C.c_uint64, vp]
         L.lgpu_get_stats.argtypes = [vp, C.POINTER(abi.Stats)]
         L.lgpu_version.restype = C.c_char_p
+        L.lgpu_probe_bandwidth.argtypes = [vp, C.c_uint64, C.c_int32, C.POINTER(C.c_double)]
         L.lgpu_scene_check.argtypes = [C.POINTER(abi.SceneDesc), C.c_char_p, C.c_size_t]
         L.lgpu_render_batch.argtypes = [vp, C.POINTER(abi.ViewDesc), C.c_int32, C.POINTER(abi.RenderOpts), vp]
         L.lgpu_adjoint.argtypes = [vp, C.POINTER(abi.CameraDesc), C.POINTER(abi.RenderOpts),
@@ -184,6 +185,13 @@ class Renderer:
         self._check(lib().lgpu_intersect(self._h, C.c_void_p(rays_ptr), C.c_void_p(hits_ptr),
                                          C.c_void_p(uv_ptr) if uv_ptr else None, n,
                                          C.c_void_p(stream) if stream else None))
+
+    def probe_bandwidth(self, nbytes, reps=20):
+        """Read bandwidth (GB/s) of a buffer of nbytes on this renderer's device (lgpu_probe_bandwidth):
+        a buffer inside L2 gives the L2 read peak, one far larger the HBM read rate."""
+        g = C.c_double(0.0)
+        self._check(lib().lgpu_probe_bandwidth(self._h, C.c_uint64(int(nbytes)), int(reps), C.byref(g)))
+        return g.value
 
     def stats(self):
         s = abi.Stats()

@@ -337,7 +337,39 @@ bool validate_scene(const HostScene &H, std::string &why) {
 
 extern "C" {
 
-LGPU_API const char *lgpu_version(void) { return "lambda-gb300 0.2 (sm_103a, BVH2, wavefront + megakernel)"; }
+LGPU_API const char *lgpu_version(void) { return "lambda-gb300 0.3 (sm_103a, BVH2, wavefront + megakernel)"; }
+
+LGPU_API int lgpu_probe_bandwidth(lgpu_context *c, uint64_t bytes, int32_t reps, double *gbs) {
+    if (!c || !gbs || reps <= 0) return LGPU_ERR_INVALID_ARG;
+    const uint64_t n4 = bytes / 16;
+    if (n4 < 1024) return fail(c, LGPU_ERR_INVALID_ARG, "probe buffer below 16 KiB");
+    cudaError_t e = cudaSetDevice(c->device);
+    float4 *buf = nullptr;
+    float *sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int sms = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e == cudaSuccess) e = cudaMalloc(&buf, n4 * 16);
+    if (e == cudaSuccess) e = cudaMalloc(&sink, sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(buf, 0, n4 * 16);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    const int blocks = sms * 8;   /* 8 resident 256-thread blocks per SM */
+    if (e == cudaSuccess) e = read_probe(buf, n4, 1, sink, blocks, 0);   /* warm-up pass */
+    if (e == cudaSuccess) e = cudaEventRecord(e0, 0);
+    if (e == cudaSuccess) e = read_probe(buf, n4, reps, sink, blocks, 0);   /* all passes in one launch */
+    if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(buf);
+    cudaFree(sink);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bandwidth probe");
+    *gbs = ms > 0.f ? (double)n4 * 16.0 * reps / (ms * 1e6) : 0.0;
+    return LGPU_OK;
+}
 
 LGPU_API int lgpu_create(lgpu_context **out, int device) {
     if (!out) return LGPU_ERR_INVALID_ARG;

@@ -836,6 +836,9 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
     int e = S.root;   /* encoded child ref of the root */
     float3 o = wo, d = wd;
     float3 inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
+#if LGPU_BOX_FMA
+    float3 oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);   /* slab distance = fma(plane, inv, -oi) */
+#endif
     float best = tmax;
     int inst_obj = -1;
     bool hit = false;
@@ -844,6 +847,9 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
     while (true) {
         if (e == LG_MARKER) {
             o = wo; d = wd; inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
+#if LGPU_BOX_FMA
+            oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+#endif
             in_blas = false; inst_obj = -1;
             if (sp == 0) break;
             e = stack[--sp];
@@ -856,12 +862,18 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
             const float4 xs = ldg4(&n->xs), ys = ldg4(&n->ys), zs = ldg4(&n->zs);
             const int4 ch = ldg4i(&n->ch);
             if (COUNT) st->nodes++;
-            const float ax0 = (xs.x - o.x) * inv.x, ax1 = (xs.y - o.x) * inv.x;
-            const float ay0 = (ys.x - o.y) * inv.y, ay1 = (ys.y - o.y) * inv.y;
-            const float az0 = (zs.x - o.z) * inv.z, az1 = (zs.y - o.z) * inv.z;
-            const float bx0 = (xs.z - o.x) * inv.x, bx1 = (xs.w - o.x) * inv.x;
-            const float by0 = (ys.z - o.y) * inv.y, by1 = (ys.w - o.y) * inv.y;
-            const float bz0 = (zs.z - o.z) * inv.z, bz1 = (zs.w - o.z) * inv.z;
+#if LGPU_BOX_FMA
+#define LG_SLAB(p, a) __fmaf_rn((p), inv.a, -oi.a)
+#else
+#define LG_SLAB(p, a) (((p) - o.a) * inv.a)
+#endif
+            const float ax0 = LG_SLAB(xs.x, x), ax1 = LG_SLAB(xs.y, x);
+            const float ay0 = LG_SLAB(ys.x, y), ay1 = LG_SLAB(ys.y, y);
+            const float az0 = LG_SLAB(zs.x, z), az1 = LG_SLAB(zs.y, z);
+            const float bx0 = LG_SLAB(xs.z, x), bx1 = LG_SLAB(xs.w, x);
+            const float by0 = LG_SLAB(ys.z, y), by1 = LG_SLAB(ys.w, y);
+            const float bz0 = LG_SLAB(zs.z, z), bz1 = LG_SLAB(zs.w, z);
+#undef LG_SLAB
             const float an = fmaxf(fmaxf(fminf(ax0, ax1), fminf(ay0, ay1)), fmaxf(fminf(az0, az1), 0.f));
             const float af = fminf(fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1)), fminf(fmaxf(az0, az1), best));
             const float bn = fmaxf(fmaxf(fminf(bx0, bx1), fminf(by0, by1)), fmaxf(fminf(bz0, bz1), 0.f));
@@ -926,6 +938,9 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
                    add_rn(add_rn(mul_rn(r1.x, wd.x), mul_rn(r1.y, wd.y)), mul_rn(r1.z, wd.z)),
                    add_rn(add_rn(mul_rn(r2.x, wd.x), mul_rn(r2.y, wd.y)), mul_rn(r2.z, wd.z)));
             inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
+#if LGPU_BOX_FMA
+            oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+#endif
             inst_obj = __ldg(&I->object);
             in_blas = true;
             if (sp + 1 > LGPU_STACK) {

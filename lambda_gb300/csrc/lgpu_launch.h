@@ -75,6 +75,7 @@ size_t wave_state_bytes_3_1();
 size_t wave_state_bytes_4_1();
 cudaError_t film_resolve(const float4 *film, float4 *rgba, uint64_t n_px, cudaStream_t st);
 cudaError_t film_reduce(const float4 *paths, float4 *film, uint64_t first_px, uint64_t n_px, int spp, cudaStream_t st);
+cudaError_t read_probe(const float4 *p, uint64_t n4, int passes, float *sink, int blocks, cudaStream_t st);
 struct AdjArgs;
 cudaError_t launch_adjoint(const DeviceScene &S, const CamParams &cam, const RenderParams &rp, const AdjArgs &A,
                            uint64_t n, cudaStream_t st);

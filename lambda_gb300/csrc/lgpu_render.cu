@@ -649,6 +649,34 @@ cudaError_t film_resolve(const float4 *film, float4 *rgba, uint64_t n_px, cudaSt
     k_film_resolve<<<(unsigned)((n_px + 255) / 256), 256, 0, st>>>(film, rgba, n_px);
     return cudaGetLastError();
 }
+/* 16-byte load cached in L2 only, issued as written (a volatile load: repeated passes over the
+ * same addresses are not merged by the compiler). */
+__device__ __forceinline__ float4 ld_cg_volatile(const float4 *p) {
+    float4 v;
+    asm volatile("ld.global.cg.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    return v;
+}
+/* Read bandwidth probe: `passes` passes over the buffer in one launch, every float4 once per pass,
+ * four independent loads per thread and step; the sum is stored only if it equals a value no
+ * buffer of zeros produces. */
+__global__ void k_read_probe(const float4 *p, uint64_t n4, int passes, float *sink) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    float acc = 0.f;
+    for (int r = 0; r < passes; ++r) {
+        uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        for (; i + 3 * stride < n4; i += 4 * stride) {
+            const float4 a = ld_cg_volatile(p + i), b = ld_cg_volatile(p + i + stride);
+            const float4 c = ld_cg_volatile(p + i + 2 * stride), d = ld_cg_volatile(p + i + 3 * stride);
+            acc += (a.x + b.y) + (c.z + d.w);
+        }
+        for (; i < n4; i += stride) acc += ld_cg_volatile(p + i).x;
+    }
+    if (acc == 1.5f) sink[0] = acc;
+}
+cudaError_t read_probe(const float4 *p, uint64_t n4, int passes, float *sink, int blocks, cudaStream_t st) {
+    k_read_probe<<<blocks, 256, 0, st>>>(p, n4, passes, sink);
+    return cudaGetLastError();
+}
 cudaError_t film_reduce(const float4 *paths, float4 *film, uint64_t first_px, uint64_t n_px, int spp, cudaStream_t st) {
     if (n_px == 0) return cudaSuccess;
     k_film_reduce<<<(unsigned)((n_px + 255) / 256), 256, 0, st>>>(paths, film, first_px, n_px, spp);

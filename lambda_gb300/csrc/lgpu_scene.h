@@ -32,6 +32,11 @@
 #ifndef LGPU_BVH_WIDE
 #define LGPU_BVH_WIDE 0
 #endif
+/* Binary-node slab distances as one fused multiply-add per plane, fma(plane, 1/d, -o/d), instead of
+ * (plane - o) * (1/d) (two roundings, two instructions without contraction). */
+#ifndef LGPU_BOX_FMA
+#define LGPU_BOX_FMA 0
+#endif
 
 /* BVH2 node (binned SAH build): child c's box is (xs[2c], xs[2c+1]) etc.
  * ch = (ref0, ref1, -, -): ref = (index << 4) | count, count 0 for an inner node, else the first
