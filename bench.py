@@ -559,6 +559,28 @@ def main_inverse(args):
     print(json.dumps(line))
 
 
+def batched_frame_rate(r, cam, opts, parts=8, steps=2):
+    """Mpath-samples/s of this frame rendered through lgpu_render_batch as `parts` views of the same
+    camera, each with spp / parts samples at successive sample offsets (together the frame's
+    samples), device films; timed with the device synchronised on both sides."""
+    import torch
+    W, H, spp = opts.width, opts.height, opts.spp
+    per = max(1, spp // parts)
+    films = [torch.zeros((H, W, 4), dtype=torch.float32, device="cuda") for _ in range(parts)]
+    views = [(cam, W, H, per, opts.max_bounces, opts.seed, f.data_ptr(), k * per) for k, f in enumerate(films)]
+    r.render_batch(views, opts)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r.render_batch(views, opts)
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / steps
+    if any(float(f[..., 3].min()) != per * (steps + 1) for f in films):
+        raise SystemExit("work check failed: batched frame sample counts")
+    del films
+    return W * H * per * parts / t / 1e6
+
+
 def relmse_record(r, cam, opts, stream, rates, threshold=1e-3, ref_spp=4096, ref_seed=777,
                   levels=(4, 8, 16, 32, 64, 128, 256, 512, 1024)):
     """Samples per pixel and wall time each renderer needs to reach relMSE <= threshold on this frame.
@@ -567,8 +589,9 @@ def relmse_record(r, cam, opts, stream, rates, threshold=1e-3, ref_spp=4096, ref
     images: the frame at growing spp (progressive passes, seed of opts).  relMSE = mean over pixels and
     channels of (I - R)^2 / (R^2 + 1e-2).  The GPU and the reference CPU integrator compute the same
     estimate per path (per-path parity), so they reach the threshold at the same spp and their times
-    to it are spp * pixels / throughput (rates: name -> Mpath-samples/s of this frame; the batched
-    record compares batched and plain on its own views at equal spp)."""
+    to it are spp * pixels / throughput (rates: name -> Mpath-samples/s of this frame, the batched
+    one from batched_frame_rate; the batched record compares batched and plain on its own uneven
+    views at equal spp)."""
     import torch
     W, H = opts.width, opts.height
     o = type(opts).from_buffer_copy(opts)
@@ -740,7 +763,7 @@ def main():
     if not args.no_extras and world == 1 and args.workload == "terrain":
         # the rest of the metric: batched vs plain, equal-relMSE times, and the adjoint's cost
         extras["batched"] = batched_record(2, 1)
-        rates = {"gpu_plain": value}
+        rates = {"gpu_plain": value, "gpu_batched": batched_frame_rate(r, cam, opts)}
         if cpu:
             rates["cpu_" + cpu["kind"]] = cpu["value"]
         extras["relmse"] = relmse_record(r, cam, opts, stream, rates)

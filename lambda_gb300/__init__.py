@@ -139,7 +139,8 @@ class Renderer:
 
     def render_batch(self, views, opts, stream=None):
         """Batched render (lgpu_render_batch).  views: list of (camera, width, height, spp,
-        max_bounces, seed, film_ptr) with film_ptr a device address of width*height float4."""
+        max_bounces, seed, film_ptr[, sample_offset]) with film_ptr a device address of
+        width*height float4."""
         arr = self._views(views)
         self._check(lib().lgpu_render_batch(self._h, arr, len(views), C.byref(opts),
                                             C.c_void_p(stream) if stream else None))
@@ -147,10 +148,11 @@ class Renderer:
     @staticmethod
     def _views(views):
         arr = (abi.ViewDesc * len(views))()
-        for i, (cam, w, h, spp, depth, seed, film_ptr) in enumerate(views):
+        for i, v in enumerate(views):
+            cam, w, h, spp, depth, seed, film_ptr = v[:7]
             arr[i].camera = cam.desc()
             arr[i].width, arr[i].height, arr[i].spp, arr[i].max_bounces = w, h, spp, depth
-            arr[i].seed, arr[i].sample_offset, arr[i].film_dev = seed, 0, film_ptr
+            arr[i].seed, arr[i].sample_offset, arr[i].film_dev = seed, (v[7] if len(v) > 7 else 0), film_ptr
         return arr
 
     def autotune(self, views, opts, probe_spp=1):
