@@ -533,11 +533,18 @@ __device__ __forceinline__ void tr_walk(const WaveArgs &W, int slot, float4 qo, 
 /* LGPU_TRACE_MINW: resident warps per SM the plain trace kernel is compiled for.  36 (56 registers
  * at 64 threads, 12 B of spills) measured 13 % faster on the 1080p terrain than the compiler's own
  * choice (64 registers, 28 warps) and 2 % faster than 40 (48 registers); 0 leaves it to the
- * compiler.  The walk kernel keeps the compiler's choice (it would spill 284 B at 56). */
+ * compiler. */
 #ifndef LGPU_TRACE_MINW
 #define LGPU_TRACE_MINW 36
 #endif
-#define LG_TRACE_MINB(BS, WALK) ((!(WALK) && LGPU_TRACE_MINW / ((BS) / 32) > 0) ? LGPU_TRACE_MINW / ((BS) / 32) : 1)
+/* LGPU_WALK_MINW: the same for the transmittance-walk kernel.  32 (64 registers, 108 B of spills)
+ * measured 1090 -> 1014 ms of traversal per 720p volume frame against the compiler's choice (80
+ * registers, 24 warps); 28 gave 1047 ms. */
+#ifndef LGPU_WALK_MINW
+#define LGPU_WALK_MINW 32
+#endif
+#define LG_MINB_OF(W, BS) ((W) / ((BS) / 32) > 0 ? (W) / ((BS) / 32) : 1)
+#define LG_TRACE_MINB(BS, WALK) ((WALK) ? LG_MINB_OF(LGPU_WALK_MINW, BS) : LG_MINB_OF(LGPU_TRACE_MINW, BS))
 
 template <bool COUNT, int BS, bool DEV, bool WALK>
 __global__ void __launch_bounds__(BS, LG_TRACE_MINB(BS, WALK)) k_wave_trace(const __grid_constant__ WaveArgs W, int lo, int n) {
