@@ -312,6 +312,10 @@ bool validate_scene(const HostScene &H, std::string &why) {
             const DLNode &n = H.lnodes[k];
             if (n.child0 == 0 || n.child0 + 1 >= (int)H.lnodes.size() || n.parent == 0 || n.parent >= (int)H.lnodes.size()) { why = "tree links"; return false; }
             if (n.child0 > 0 && (n.child0 & 1)) { why = "tree sibling pair alignment"; return false; }
+            if (n.child0 > 0 && (H.lnodes[n.child0].parent != (int)k || H.lnodes[n.child0 + 1].parent != (int)k)) {
+                why = "tree parent links";   /* the pdf walk climbs by parent and reads the sibling at index ^ 1 */
+                return false;
+            }
             if (n.first < 0 || n.num < 1 || n.first + n.num > (int)H.treeLights.size()) { why = "tree light range"; return false; }
             if (n.child0 < 0 && (n.dist_off < 0 || (size_t)n.dist_off + 2 * n.num + 1 > fp)) { why = "tree leaf cdf"; return false; }
         }
@@ -383,7 +387,9 @@ LGPU_API int lgpu_create(lgpu_context **out, int device) {
     std::memset(&c->stats, 0, sizeof(c->stats));
     std::memset(&c->S, 0, sizeof(c->S));
     e = cudaSetDevice(device);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, 4 * sizeof(unsigned long long));
+    /* traversal counters (4) and, in the state-clock diagnostic build, cycles per program point (32) */
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_counters, 36 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(c->d_counters, 0, 36 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
@@ -1293,6 +1299,22 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     c->stats.pool_slots = (uint32_t)slots;
     c->stats.spawned += n;
     c->stats.launches += launches;
+#ifdef LGPU_STATE_CLOCKS
+    {   /* diagnostic build: cycles per program point of this render, to stderr */
+        static const char *names[] = {"NEW", "LOOP", "TOP_HIT", "MISS", "BODY", "SURF_A", "SURF_LI", "SURF_EXT",
+                                      "NULL_EXT", "RR", "NEXT_ITER", "MED_A", "LDM_START", "LDM_VIS", "LDM_SCAT",
+                                      "MED_EXT", "VIS_OCCL", "VIS_TR", "TR_STEP", "DONE"};
+        unsigned long long h[32];
+        if (cudaMemcpyAsync(h, c->d_counters + 4, sizeof(h), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+            cudaStreamSynchronize(st) == cudaSuccess) {
+            std::fprintf(stderr, "state-clock (lane-0 cycles, G):");
+            for (int k = 0; k < 20; ++k)
+                if (h[k]) std::fprintf(stderr, " %s=%.2f", names[k], (double)h[k] * 1e-9);
+            std::fprintf(stderr, "\n");
+        }
+        cudaMemsetAsync(c->d_counters + 4, 0, 32 * sizeof(unsigned long long), st);
+    }
+#endif
     return check_device_error(c, st);
 }
 

@@ -440,9 +440,10 @@ struct Tracer {
             eps /= pTree;
             *pdf *= pTree;
             float e = rng.next();   /* B6: a fresh draw drives the descent */
-            int ni = S.tree_root;
+            /* the chosen child's record, loaded with its sibling, is the next level's node: one
+             * round of (two independent) loads per level */
+            DLNode n = S.lnodes[S.tree_root];
             for (int guard = 0; guard < 64; ++guard) {
-                const DLNode &n = S.lnodes[ni];
                 if (n.child0 < 0) {
                     const float *cdf = S.fpool + n.dist_off;
                     const int off = find_interval(cdf, n.num + 1, e);
@@ -454,8 +455,8 @@ struct Tracer {
                 const float IR = importance(p, nS, cr);
                 const float PL = IL / (IL + IR);
                 const float PR = 1.f - PL;
-                if (e < PL) { e /= PL; *pdf *= PL; ni = n.child0; }
-                else { e = (e - PL) / PR; *pdf *= PR; ni = n.child0 + 1; }
+                if (e < PL) { e /= PL; *pdf *= PL; n = cl; }
+                else { e = (e - PL) / PR; *pdf *= PR; n = cr; }
             }
         }
         *pdf *= 1.f - pTree;
@@ -475,22 +476,24 @@ struct Tracer {
         } else ti = S.light_slot[l.light];
         if (ti < 0 || ti >= S.num_tree_lights) return 0.f;
         const int2 slot = __ldg(&S.tree_slot[ti]);
-        const DLNode &leaf = S.lnodes[slot.x];
-        const float pdf = S.fpool[leaf.dist_off + leaf.num + 1 + slot.y];   /* raw power (Piecewise1D::PDF) */
+        DLNode cur = S.lnodes[slot.x];
+        const float pdf = S.fpool[cur.dist_off + cur.num + 1 + slot.y];   /* raw power (Piecewise1D::PDF) */
         /* branch probabilities multiplied leaf-up (the reference's recursion multiplies root-down;
-         * the two orders agree to a few ulps) */
+         * the two orders agree to a few ulps).  Sibling pairs are (even, even + 1) records, so the
+         * sibling is index ^ 1 and the left child is the even one; the sibling and the parent are
+         * independent loads of each level. */
         int child = slot.x;
-        int ni = leaf.parent;
         float acc = 1.f;
-        for (int depth = 0; ni >= 0 && depth < LG_MAX_TREE_DEPTH; ++depth) {
-            const DLNode &n = S.lnodes[ni];
-            const DLNode cl = S.lnodes[n.child0], cr = S.lnodes[n.child0 + 1];
-            const float IL = importance(p, nS, cl);
-            const float IR = importance(p, nS, cr);
+        for (int depth = 0; cur.parent >= 0 && depth < LG_MAX_TREE_DEPTH; ++depth) {
+            const DLNode sib = S.lnodes[child ^ 1];
+            const DLNode par = S.lnodes[cur.parent];
+            const bool left = (child & 1) == 0;
+            const float IL = importance(p, nS, left ? cur : sib);
+            const float IR = importance(p, nS, left ? sib : cur);
             const float p0 = IL / (IL + IR);
-            acc = ((child == n.child0) ? p0 : 1.f - p0) * acc;
-            child = ni;
-            ni = n.parent;
+            acc = (left ? p0 : 1.f - p0) * acc;
+            child = cur.parent;
+            cur = par;
         }
         return pdf * acc;
     }

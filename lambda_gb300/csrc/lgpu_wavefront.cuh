@@ -137,6 +137,26 @@ struct WaveArgs {
     int fold_tr;
 };
 
+#ifdef LGPU_STATE_CLOCKS
+/* Diagnostic build: SM cycles spent in each program point of Wave::run, sampled on lane 0 of every
+ * warp and added into clk[pc] (the context's counter block past the traversal counters). */
+struct StateClock {
+    unsigned long long *clk;
+    int pc = -1;
+    long long t = 0;
+    bool on;
+    __device__ explicit StateClock(unsigned long long *c) : clk(c), on(c && (threadIdx.x & 31) == 0) {}
+    __device__ void tick(int next) {
+        if (!on) return;
+        const long long now = clock64();
+        if (pc >= 0 && pc < 32) atomicAdd(&clk[pc], (unsigned long long)(now - t));
+        pc = next;
+        t = now;
+    }
+    __device__ ~StateClock() { tick(-1); }
+};
+#endif
+
 /* Append `slot` to segment `seg` of the next queue; one atomic per group of lanes with the same
  * segment. */
 __device__ __forceinline__ void push_queue(const WaveArgs &W, int slot, int seg) {
@@ -411,7 +431,13 @@ struct Wave {
         const DeviceScene &S = W.S;
         const RenderParams &rp = W.views ? W.views[s.view].rp : W.rp;
         const int maxB = rp.max_bounces, minB = rp.min_bounces;
+#ifdef LGPU_STATE_CLOCKS
+        StateClock clk(W.counters ? W.counters + 4 : nullptr);
+#endif
         for (int guard = 0; guard < 4096; ++guard) {
+#ifdef LGPU_STATE_CLOCKS
+            clk.tick(s.pc);
+#endif
             switch (s.pc) {
             case PC_LOOP: {
                 if (s.bounces >= maxB) { s.pc = PC_DONE; break; }
