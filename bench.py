@@ -559,6 +559,36 @@ def main_inverse(args):
     print(json.dumps(line))
 
 
+def device_bvh_record(sb, cam, opts, steps=2):
+    """The same frame on a BVH built on the device (lgpu_set_bvh_builder, LBVH): its build time for
+    the scene's triangles, its node count beside the host SAH tree's, and the frame's throughput."""
+    import torch
+    import lambda_gb300 as lg
+    from lambda_gb300 import abi
+    W, H, spp = opts.width, opts.height, opts.spp
+    r = lg.Renderer(sb, bvh_builder=abi.BVH_BUILD_DEVICE)
+    try:
+        st = r.stats()
+        film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        r.render_device(cam, opts, film.data_ptr())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            r.render_device(cam, opts, film.data_ptr())
+        torch.cuda.synchronize()
+        t = (time.perf_counter() - t0) / steps
+        if float(film[..., 3].min()) != spp * (steps + 1):
+            raise SystemExit("work check failed: device-BVH frame sample counts")
+        d = sb.desc()
+        return {"build_ms": st["bvh_build_ms"], "bvh_nodes": st["bvh_nodes"],
+                "triangles": sum(d.meshes[k].num_triangles for k in range(d.num_meshes)),
+                "frame_ms": t * 1e3, "value": W * H * spp / t / 1e6,
+                "builder": "device LBVH: 30-bit Morton codes, radix sort, radix tree, bottom-up boxes, one "
+                           "triangle per leaf (the default is the host's binned-SAH build)"}
+    finally:
+        r.close()
+
+
 def batched_frame_rate(r, cam, opts, parts=8, steps=2):
     """Mpath-samples/s of this frame rendered through lgpu_render_batch as `parts` views of the same
     camera, each with spp / parts samples at successive sample offsets (together the frame's
@@ -768,6 +798,7 @@ def main():
             rates["cpu_" + cpu["kind"]] = cpu["value"]
         extras["relmse"] = relmse_record(r, cam, opts, stream, rates)
         extras["adjoint"] = inverse_record(4, 1)
+        extras["device_bvh"] = device_bvh_record(sb, cam, opts)
     cfg["l2"] = "scene data > L2 and a 256 MiB buffer is written between timed steps"
     cfg["width"], cfg["height"], cfg["spp"] = W, H, spp
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -317,6 +317,7 @@ typedef struct lgpu_stats {
     uint64_t traced;          /* ray queries answered by the trace kernel */
     uint64_t spawned;         /* paths started */
     uint64_t launches;        /* kernels launched by the last render */
+    double bvh_build_ms;      /* device time of the last commit's BVH builds (device builder only) */
 } lgpu_stats;
 
 typedef struct lgpu_context lgpu_context;
@@ -492,6 +493,14 @@ LGPU_API const char *lgpu_version(void);
  * A buffer well inside L2 (e.g. 32 MiB) gives the L2 read peak that the traversal kernels are
  * compared against; one well beyond it gives the HBM read rate.  No counterpart in the reference. */
 LGPU_API int lgpu_probe_bandwidth(lgpu_context *ctx, uint64_t bytes, int32_t reps, double *gbs);
+
+/* BVH builder of the following commits: LGPU_BVH_BUILD_HOST (default) builds binned-SAH trees on
+ * the host; LGPU_BVH_BUILD_DEVICE builds linear BVHs on the device (Morton order, radix tree,
+ * bottom-up boxes; one primitive per leaf) in milliseconds, at some cost in traversal.  Both give
+ * the same node layout and the same hits.  Replaces rtcCommitScene's build (src/core/Scene.cpp:18-26)
+ * for the GPU path; lgpu_stats::bvh_build_ms reports the device build time. */
+typedef enum lgpu_bvh_build { LGPU_BVH_BUILD_HOST = 0, LGPU_BVH_BUILD_DEVICE = 1 } lgpu_bvh_build;
+LGPU_API int lgpu_set_bvh_builder(lgpu_context *ctx, int32_t builder);
 
 #ifdef __cplusplus
 }

@@ -19,7 +19,7 @@ LIB_PATH = pathlib.Path(os.environ["LGPU_LIB_PATH"]) if os.environ.get("LGPU_LIB
 EXPORTS = ["lgpu_create", "lgpu_destroy", "lgpu_last_error", "lgpu_scene_commit", "lgpu_render",
            "lgpu_render_device", "lgpu_render_paths", "lgpu_render_count", "lgpu_intersect",
            "lgpu_get_stats", "lgpu_version", "lgpu_scene_check", "lgpu_render_paths_noalloc", "lgpu_render_batch", "lgpu_autotune", "lgpu_adjoint", "lgpu_film_resolve",
-           "lgpu_render_progressive", "lgpu_probe_bandwidth"]
+           "lgpu_render_progressive", "lgpu_probe_bandwidth", "lgpu_set_bvh_builder"]
 
 _lib = None
 
@@ -60,6 +60,7 @@ def lib():
         L.lgpu_get_stats.argtypes = [vp, C.POINTER(abi.Stats)]
         L.lgpu_version.restype = C.c_char_p
         L.lgpu_probe_bandwidth.argtypes = [vp, C.c_uint64, C.c_int32, C.POINTER(C.c_double)]
+        L.lgpu_set_bvh_builder.argtypes = [vp, C.c_int32]
         L.lgpu_scene_check.argtypes = [C.POINTER(abi.SceneDesc), C.c_char_p, C.c_size_t]
         L.lgpu_render_batch.argtypes = [vp, C.POINTER(abi.ViewDesc), C.c_int32, C.POINTER(abi.RenderOpts), vp]
         L.lgpu_adjoint.argtypes = [vp, C.POINTER(abi.CameraDesc), C.POINTER(abi.RenderOpts),
@@ -88,7 +89,8 @@ def _ptr(a):
 class Renderer:
     """One GPU context holding one committed scene (lgpu_create + lgpu_scene_commit)."""
 
-    def __init__(self, scene, device=0):
+    def __init__(self, scene, device=0, bvh_builder=0):
+        """bvh_builder: abi.BVH_BUILD_HOST (binned SAH on the host) or abi.BVH_BUILD_DEVICE (LBVH)."""
         L = lib()
         h = C.c_void_p()
         rc = L.lgpu_create(C.byref(h), device)
@@ -97,6 +99,8 @@ class Renderer:
         self._h = h
         self._desc = scene.desc()
         self._scene = scene
+        if bvh_builder:
+            self._check(L.lgpu_set_bvh_builder(self._h, int(bvh_builder)))
         self._check(L.lgpu_scene_commit(self._h, C.byref(self._desc)))
 
     def _check(self, rc):

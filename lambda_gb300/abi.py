@@ -111,6 +111,7 @@ class RenderOpts(C.Structure):
 
 
 KERNEL_AUTO, KERNEL_MEGAKERNEL, KERNEL_WAVEFRONT, KERNEL_WAVEFRONT_GRAPH = 0, 1, 2, 3
+BVH_BUILD_HOST, BVH_BUILD_DEVICE = 0, 1
 
 
 class Stats(C.Structure):
@@ -121,7 +122,7 @@ class Stats(C.Structure):
                 ("trace_ms", C.c_double), ("shade_ms", C.c_double), ("spawn_ms", C.c_double),
                 ("iterations", C.c_uint32), ("pool_slots", C.c_uint32), ("stage_ms", C.c_double * 6),
                 ("resumed", C.c_uint64 * 6), ("traced", C.c_uint64), ("spawned", C.c_uint64),
-                ("launches", C.c_uint64)]
+                ("launches", C.c_uint64), ("bvh_build_ms", C.c_double)]
 
 
 def render_opts(width, height, spp, max_bounces, min_bounces=3, seed=1, spectral=SPECTRAL_RGB3,

@@ -21,7 +21,7 @@ LIB = OUT / "liblambda_gpu.so"
 _PARTS = [(ns, cnt, part) for ns in (3, 4) for cnt in (0, 1) for part in (1, 2, 3, 4, 5)
           if (part != 3 or ns == 3) and (part != 4 or (ns == 3 and cnt == 0))]
 SOURCES = [("lgpu_api.cu", [], "lgpu_api"), ("lgpu_compile.cu", [], "lgpu_compile"),
-           ("lgpu_lighttree.cpp", [], "lgpu_lighttree")] + [
+           ("lgpu_lighttree.cpp", [], "lgpu_lighttree"), ("lgpu_lbvh.cu", [], "lgpu_lbvh")] + [
     ("lgpu_render.cu", ["-DLGPU_NS=%d" % ns, "-DLGPU_COUNT=%d" % cnt, "-DLGPU_PART=%d" % part],
      "render_%d_%d_p%d" % (ns, cnt, part)) for ns, cnt, part in _PARTS]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

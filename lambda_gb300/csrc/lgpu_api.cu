@@ -36,6 +36,8 @@ using namespace lg;
 
 struct lgpu_context {
     int device = 0;
+    int bvh_builder = LGPU_BVH_BUILD_HOST;   /* lgpu_set_bvh_builder */
+    double bvh_build_ms = 0;                 /* device time of the last commit's BVH builds */
     std::string err;
     std::vector<void *> scene_allocs;
     DeviceScene S;
@@ -343,6 +345,16 @@ extern "C" {
 
 LGPU_API const char *lgpu_version(void) { return "lambda-gb300 0.3 (sm_103a, BVH2, wavefront + megakernel)"; }
 
+LGPU_API int lgpu_set_bvh_builder(lgpu_context *c, int32_t builder) {
+    if (!c) return LGPU_ERR_INVALID_ARG;
+    if (builder != LGPU_BVH_BUILD_HOST && builder != LGPU_BVH_BUILD_DEVICE) return fail(c, LGPU_ERR_INVALID_ARG, "unknown BVH builder");
+#if LGPU_BVH_WIDE
+    if (builder == LGPU_BVH_BUILD_DEVICE) return fail(c, LGPU_ERR_INVALID_ARG, "the device builder writes binary nodes; this build uses 8-wide nodes");
+#endif
+    c->bvh_builder = builder;
+    return LGPU_OK;
+}
+
 LGPU_API int lgpu_probe_bandwidth(lgpu_context *c, uint64_t bytes, int32_t reps, double *gbs) {
     if (!c || !gbs || reps <= 0) return LGPU_ERR_INVALID_ARG;
     const uint64_t n4 = bytes / 16;
@@ -563,6 +575,23 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
         return b;
     };
     int maxDepth = 0;
+    c->bvh_build_ms = 0;
+    /* one BVH: the host's binned SAH, or the device's LBVH when selected (binary layout only) */
+    std::string bvh_err;
+    auto bvh = [&](const std::vector<Aabb> &boxes, int max_leaf, int node_base, int prim_base, DeviceBvh &out) -> bool {
+#if !LGPU_BVH_WIDE
+        if (c->bvh_builder == LGPU_BVH_BUILD_DEVICE && boxes.size() >= 2) {
+            BvhOut b;
+            float ms = 0.f;
+            if (build_lbvh_device(boxes, node_base, prim_base, b, &ms, bvh_err) != 0) return false;
+            c->bvh_build_ms += ms;
+            out.nodes.swap(b.nodes); out.order.swap(b.order); out.root_ref = b.root_ref; out.depth = b.max_depth;
+            return true;
+        }
+#endif
+        build_device_bvh(boxes, max_leaf, node_base, prim_base, out);
+        return true;
+    };
     /* world BLAS over plain mesh objects */
     std::vector<std::pair<int, uint32_t>> worldPrims;   /* (object, triangle) */
     bool anyInstance = false;
@@ -576,7 +605,7 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
         std::vector<Aabb> boxes(worldPrims.size());
         for (size_t k = 0; k < worldPrims.size(); ++k) boxes[k] = tri_box(d->meshes[d->objects[worldPrims[k].first].mesh], worldPrims[k].second);
         DeviceBvh bo;
-        build_device_bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo);
+        if (!bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo)) return fail(c, LGPU_ERR_CUDA, bvh_err);
         maxDepth = std::max(maxDepth, bo.depth);
         nodes.insert(nodes.end(), bo.nodes.begin(), bo.nodes.end());
         for (uint32_t k : bo.order) {
@@ -611,7 +640,7 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
                 std::vector<Aabb> boxes(m.num_triangles);
                 for (uint32_t t = 0; t < m.num_triangles; ++t) boxes[t] = tri_box(m, t);
                 DeviceBvh bo;
-                build_device_bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo);
+                if (!bvh(boxes, 4, (int)nodes.size(), (int)tris.size(), bo)) return fail(c, LGPU_ERR_CUDA, bvh_err);
                 maxDepth = std::max(maxDepth, bo.depth);
                 nodes.insert(nodes.end(), bo.nodes.begin(), bo.nodes.end());
                 for (uint32_t k : bo.order) tris.push_back(make_tri(m, k, -1));
@@ -634,7 +663,7 @@ int compile_scene(lgpu_context *c, const lgpu_scene_desc *d, HostScene &H) {
             instBoxes.push_back(ab);
         }
         DeviceBvh bo;
-        build_device_bvh(instBoxes, 1, (int)nodes.size(), 0, bo);
+        if (!bvh(instBoxes, 1, (int)nodes.size(), 0, bo)) return fail(c, LGPU_ERR_CUDA, bvh_err);
         nodes.insert(nodes.end(), bo.nodes.begin(), bo.nodes.end());
         std::vector<DInst> reordered;
         for (uint32_t k : bo.order) reordered.push_back(insts[k]);
@@ -963,6 +992,7 @@ LGPU_API int lgpu_scene_commit(lgpu_context *c, const lgpu_scene_desc *d) {
     c->num_materials = (int)H.mats.size();
     c->have_scene = true;
     c->stats.bvh_nodes = nodes.size();
+    c->stats.bvh_build_ms = c->bvh_build_ms;
     c->stats.bvh_bytes = nodes.size() * sizeof(BvhNode);
     c->stats.tri_bytes = tris.size() * sizeof(DTri);
     c->stats.node_bytes = sizeof(BvhNode);

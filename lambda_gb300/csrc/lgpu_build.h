@@ -62,6 +62,12 @@ inline void build_device_bvh(const std::vector<Aabb> &boxes, int max_leaf, int n
 #endif
 }
 
+/* Linear BVH built on the device (Morton codes, sort, radix tree, bottom-up boxes), written as
+ * binary nodes with one primitive per leaf in the numbering of build_bvh.  Needs >= 2 boxes and a
+ * current CUDA device; *device_ms receives the device time.  Returns 0 or an error code (err). */
+int build_lbvh_device(const std::vector<Aabb> &boxes, int node_base, int prim_base, BvhOut &out, float *device_ms,
+                      std::string &err);
+
 /* Shader-graph compiler: DAG -> linear bytecode with one register per live value. */
 struct GraphCompiler {
     const lgpu_scene_desc *d = nullptr;
