@@ -836,6 +836,7 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
     int e = S.root;   /* encoded child ref of the root */
     float3 o = wo, d = wd;
     float3 inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    const float3 winv = inv;   /* world-space 1/d, restored when the ray leaves an instance */
 #if LGPU_BOX_FMA
     float3 oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);   /* slab distance = fma(plane, inv, -oi) */
 #endif
@@ -846,7 +847,7 @@ __device__ __forceinline__ bool traverse_t(const DeviceScene &S, float3 wo, floa
     if (COUNT) st->rays++;
     while (true) {
         if (e == LG_MARKER) {
-            o = wo; d = wd; inv = mk(1.f / d.x, 1.f / d.y, 1.f / d.z);
+            o = wo; d = wd; inv = winv;
 #if LGPU_BOX_FMA
             oi = mk(o.x * inv.x, o.y * inv.y, o.z * inv.z);
 #endif
