@@ -280,7 +280,7 @@ typedef struct lgpu_render_opts {
     uint32_t sample_offset;   /* first sample index: resume = same seed, offset = samples done */
     int32_t block_size;       /* threads per block of the wavefront trace kernel: 64, 128, 256 or 512 (0 = 64) */
     int32_t kernel_mode;      /* lgpu_kernel_mode */
-    int32_t pool_slots;       /* wavefront path-slot pool size, 0 = default (4 Mi slots) */
+    int32_t pool_slots;       /* wavefront path-slot pool size, 0 = default (8 Mi slots) */
 } lgpu_render_opts;
 
 /* Execution scheme of one render.  Both produce the same paths (same random-number order). */

