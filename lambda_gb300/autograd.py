@@ -11,8 +11,10 @@ differentiable function of
 
 Forward: the scene is committed with the given values and rendered on the GPU by the wavefront
 (per path the same estimate as the megakernel that the adjoint replays, with the film summed in a
-fixed order, so repeated renders are bit-identical).  Backward: `lgpu_adjoint` with dLoss/dI =
-the incoming gradient, on the same committed scene, seed and samples.  The gradient is that of this Monte Carlo
+fixed order, so repeated renders are bit-identical); the context is released before returning, so
+a graph that is never differentiated holds no device memory.  Backward: the same scene is
+committed again from its host-side description (the compile is deterministic) and
+`lgpu_adjoint` runs with dLoss/dI = the incoming gradient, on the same seed and samples.  The gradient is that of this Monte Carlo
 estimate with its samples held fixed (plus the validity score the adjoint documents), not a
 finite difference.  RGB3 only, as lgpu_adjoint.
 """
@@ -37,17 +39,16 @@ class _Render(torch.autograd.Function):
         try:
             r.render_device(camera, opts, film.data_ptr())
             torch.cuda.synchronize()
-        except Exception:
+        finally:
             r.close()
-            raise
-        ctx.renderer, ctx.camera, ctx.opts, ctx.params = r, camera, opts, tuple(params)
+        ctx.scene, ctx.camera, ctx.opts, ctx.params = sb, camera, opts, tuple(params)
         ctx.tex_shape = tuple(albedo.shape)
         ctx.devices = (albedo.device, scalars.device)
         return film[..., :3] / film[..., 3:4]
 
     @staticmethod
     def backward(ctx, grad_img):
-        r = ctx.renderer
+        r = Renderer(ctx.scene)
         h, w = ctx.opts.height, ctx.opts.width
         try:
             dloss = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
@@ -59,7 +60,6 @@ class _Render(torch.autograd.Function):
             torch.cuda.synchronize()
         finally:
             r.close()
-            ctx.renderer = None
         return gtex[..., :3].to(ctx.devices[0]), gsc.to(ctx.devices[1]), None, None, None, None
 
 
